@@ -1,0 +1,319 @@
+"""gfirst_gb300 -- GB300 (sm_103a) implementation of GFIRST's OSEM hot path.
+
+The product is the C-ABI library lib/libgfirst.so (include/gfirst.h) and the
+`gfirst` command line (lib/gfirst), a drop-in for the reference program's
+four modes.  This module is a thin ctypes front end over that C-ABI; it never
+computes anything itself and raises if the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "lib" / "libgfirst.so"
+CLI_PATH = _HERE / "lib" / "gfirst"
+
+STATUS = {0: "GF_OK", 1: "GF_ERR_ARG", 2: "GF_ERR_GEOMETRY", 3: "GF_ERR_CUDA", 4: "GF_ERR_NOMEM",
+          5: "GF_ERR_IO", 6: "GF_ERR_STATE", 7: "GF_ERR_NODEV", 8: "GF_ERR_TIMEOUT"}
+
+
+class GfError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class _CGeom(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in ("res", "nzs", "nrad", "nang", "span", "nseg")] + \
+               [(n, ctypes.c_float) for n in ("pitch_mm", "diam_det_mm", "fov_mm")]
+
+
+class _CParams(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("niter", ctypes.c_int32), ("psf_fw", ctypes.c_float),
+                ("psf_bw", ctypes.c_float), ("scale_d", ctypes.c_float), ("scale_t", ctypes.c_float)]
+
+
+@dataclass(frozen=True)
+class Geometry:
+    """The compile-time constants of GFIRST.h:4-36, chosen at run time."""
+    res: int
+    nzs: int
+    nrad: int
+    nang: int
+    span: int
+    nseg: int
+    pitch: float
+    diam: float
+    fov: float
+
+    def c(self) -> _CGeom:
+        return _CGeom(self.res, self.nzs, self.nrad, self.nang, self.span, self.nseg, self.pitch, self.diam, self.fov)
+
+    def tuple(self) -> tuple:
+        return (self.res, self.nzs, self.nrad, self.nang, self.span, self.nseg, self.pitch, self.diam, self.fov)
+
+    @staticmethod
+    def reference() -> "Geometry":
+        """GFIRST.h as compiled: Inveon, 128x128x159, 147x168, span 11, 15 segments."""
+        return Geometry(128, 159, 147, 168, 11, 15, 1.63, 165.7758, 100.0)
+
+    @staticmethod
+    def small() -> "Geometry":
+        """64x64x32 image of 0.8 mm, 64 radial x 64 angles, span 3, 11 segments (192 planes)."""
+        return Geometry(64, 32, 64, 64, 3, 11, 1.6, 84.8772096, 51.2)
+
+    @staticmethod
+    def preclinical() -> "Geometry":
+        """128x128x159 image (0.78 x 0.78 x 0.8 mm), 128 radial x 160 angles, span 3, 53 segments (4319 planes)."""
+        return Geometry(128, 159, 128, 160, 3, 53, 1.6, 165.7758, 100.0)
+
+
+def _load() -> ctypes.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(str(LIB_PATH))
+    lib.gf_last_error.restype = ctypes.c_char_p
+    for name in ("gf_create", "gf_destroy", "gf_device_alloc"):
+        getattr(lib, name)
+    lib.gf_destroy.restype = None
+    lib.gf_recon_destroy.restype = None
+    lib.gf_copy_to_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+    lib.gf_copy_to_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+    lib.gf_device_alloc.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
+    lib.gf_device_free.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    return lib
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = _load()
+    return _lib
+
+
+def _ck(st: int) -> None:
+    if st != 0:
+        raise GfError(st, lib().gf_last_error().decode())
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def sizes(g: Geometry) -> tuple:
+    p, nd, nv = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    _ck(lib().gf_geometry_sizes(ctypes.byref(g.c()), ctypes.byref(p), ctypes.byref(nd), ctypes.byref(nv)))
+    return p.value, nd.value, nv.value
+
+
+def segment_table(g: Geometry):
+    idz, zmin, acc = (np.zeros(g.nseg, np.int32), np.zeros(g.nseg, np.int32), np.zeros(g.nseg + 1, np.int32))
+    _ck(lib().gf_segment_table(ctypes.byref(g.c()), _ptr(idz), _ptr(zmin), _ptr(acc)))
+    return idz, zmin, acc
+
+
+def lor_index(g: Geometry, seg: int, iz0: int, theta: int, ird: int) -> int:
+    out = ctypes.c_int64()
+    _ck(lib().gf_lor_index(ctypes.byref(g.c()), seg, iz0, theta, ird, ctypes.byref(out)))
+    return out.value
+
+
+class DeviceArray:
+    """A device buffer owned through the C-ABI's allocation helpers."""
+
+    def __init__(self, ctx: "Context", n: int, dtype=np.float32):
+        self.ctx, self.n, self.dtype = ctx, int(n), np.dtype(dtype)
+        p = ctypes.c_void_p()
+        _ck(lib().gf_device_alloc(ctx.h, self.nbytes, ctypes.byref(p)))
+        self.p = p
+
+    @property
+    def nbytes(self) -> int:
+        return self.n * self.dtype.itemsize
+
+    def upload(self, a: np.ndarray) -> "DeviceArray":
+        a = np.ascontiguousarray(a, dtype=self.dtype).ravel()
+        assert a.size == self.n
+        _ck(lib().gf_copy_to_device(self.ctx.h, self.p, _ptr(a), self.nbytes))
+        return self
+
+    def download(self) -> np.ndarray:
+        out = np.empty(self.n, self.dtype)
+        _ck(lib().gf_copy_to_host(self.ctx.h, _ptr(out), self.p, self.nbytes))
+        return out
+
+    def zero(self) -> "DeviceArray":
+        return self.upload(np.zeros(self.n, self.dtype))
+
+    def free(self) -> None:
+        if self.p:
+            lib().gf_device_free(self.ctx.h, self.p)
+            self.p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    """gf_ctx: geometry, subsets and a stream on one device."""
+
+    def __init__(self, g: Geometry, nsub: int = 1, device: int = 0):
+        self.g, self.nsub = g, nsub
+        self.P, self.ndata, self.nvox = sizes(g)
+        h = ctypes.c_void_p()
+        _ck(lib().gf_create(ctypes.byref(g.c()), nsub, device, ctypes.byref(h)))
+        self.h = h
+
+    def close(self) -> None:
+        if self.h:
+            lib().gf_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def array(self, n: int, dtype=np.float32) -> DeviceArray:
+        return DeviceArray(self, n, dtype)
+
+    def put(self, a: np.ndarray, dtype=np.float32) -> DeviceArray:
+        a = np.ascontiguousarray(a, dtype=dtype).ravel()
+        return DeviceArray(self, a.size, dtype).upload(a)
+
+    def sync(self) -> None:
+        _ck(lib().gf_synchronize(self.h))
+
+    # operators on device arrays (reference file layouts)
+    def forward_project(self, img: DeviceArray, subset: int, proj: DeviceArray) -> None:
+        _ck(lib().gf_forward_project(self.h, img.p, subset, proj.p))
+
+    def ratio(self, proj, data, bg, subset, corr) -> None:
+        _ck(lib().gf_ratio(self.h, proj.p, data.p, bg.p, subset, corr.p))
+
+    def norm_mask(self, proj_blank, blank, calib) -> None:
+        _ck(lib().gf_norm_mask(self.h, proj_blank.p, blank.p, calib.p))
+
+    def back_project(self, corr, calib, subset, numer, denom) -> None:
+        _ck(lib().gf_back_project(self.h, corr.p, calib.p, subset, numer.p, denom.p))
+
+    def psf_xy(self, src, psf, dst) -> None:
+        _ck(lib().gf_psf_xy(self.h, src.p, ctypes.c_float(psf), dst.p))
+
+    def image_update(self, img, numer, denom, psf_bw=1.5) -> None:
+        _ck(lib().gf_image_update(self.h, img.p, numer.p, denom.p, ctypes.c_float(psf_bw)))
+
+    def bilateral(self, src, ref, max_ref, dst, r=4, sigma3d=0.75, sigmai=0.025) -> None:
+        _ck(lib().gf_bilateral(self.h, src.p, ref.p, ctypes.c_float(max_ref), r, ctypes.c_float(sigma3d),
+                               ctypes.c_float(sigmai), dst.p))
+
+    def vlor_count(self, ev, nev, cnt) -> None:
+        _ck(lib().gf_vlor_count(self.h, ev.p, ctypes.c_int64(nev), cnt.p))
+
+    def vlor_split(self, ev, nev, proj, blankt, out) -> None:
+        _ck(lib().gf_vlor_split(self.h, ev.p, ctypes.c_int64(nev), proj.p, blankt.p, out.p))
+
+
+def recon_defaults(mode: int) -> _CParams:
+    p = _CParams()
+    _ck(lib().gf_recon_defaults(mode, ctypes.byref(p)))
+    return p
+
+
+class Recon:
+    """gf_recon: one reconstruction of a CLI mode, resident on the device."""
+
+    def __init__(self, ctx: Context, mode: int, niter: int = 60, psf_fw: float = 1.5, psf_bw: float = 1.5):
+        self.ctx, self.mode = ctx, mode
+        p = recon_defaults(mode)
+        p.niter, p.psf_fw, p.psf_bw = niter, psf_fw, psf_bw
+        self.params = p
+        h = ctypes.c_void_p()
+        _ck(lib().gf_recon_create(ctx.h, ctypes.byref(p), ctypes.byref(h)))
+        self.h = h
+
+    def close(self) -> None:
+        if self.h:
+            lib().gf_recon_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def load(self, image=None, dsino=None, tsino=None, norm=None, events=None) -> None:
+        f32 = lambda a: None if a is None else np.ascontiguousarray(a, np.float32).ravel()  # noqa: E731
+        image, dsino, tsino, norm = f32(image), f32(dsino), f32(tsino), f32(norm)
+        ev = None if events is None else np.ascontiguousarray(events, np.int32)
+        nev = 0 if ev is None else ev.size // 2
+        self._keep = (image, dsino, tsino, norm, ev)
+        p = lambda a: None if a is None else _ptr(a)  # noqa: E731
+        _ck(lib().gf_recon_load(self.h, p(image), p(dsino), p(tsino), p(norm), p(ev), ctypes.c_int64(nev)))
+
+    def iterate(self, n: int = 1) -> None:
+        _ck(lib().gf_recon_iterate(self.h, n))
+
+    def subiteration(self) -> None:
+        _ck(lib().gf_recon_subiteration(self.h))
+
+    def image(self, typ: int = 0, scaled: bool = False) -> np.ndarray:
+        out = np.empty(self.ctx.nvox, np.float32)
+        _ck(lib().gf_recon_get_image(self.h, typ, int(scaled), _ptr(out)))
+        return out
+
+    def proj_ref(self) -> np.ndarray:
+        out = np.empty(self.ctx.ndata, np.float32)
+        _ck(lib().gf_recon_get_proj_ref(self.h, _ptr(out)))
+        return out
+
+    def sinog_vlor(self) -> np.ndarray:
+        out = np.empty(self.ctx.ndata, np.float32)
+        _ck(lib().gf_recon_get_sinog_vlor(self.h, _ptr(out)))
+        return out
+
+
+def read_sinogram(path, ndata: int):
+    out = np.empty(2 * ndata, np.float32)
+    st = lib().gf_read_sinogram(str(path).encode(), ctypes.c_int64(ndata), _ptr(out))
+    return out, st
+
+
+def read_vlor(path) -> np.ndarray:
+    n = ctypes.c_int64()
+    _ck(lib().gf_read_vlor(str(path).encode(), None, ctypes.byref(n)))
+    out = np.zeros(max(1, n.value) * 2, np.int32)
+    _ck(lib().gf_read_vlor(str(path).encode(), _ptr(out), ctypes.byref(n)))
+    return out[: 2 * n.value].reshape(-1, 2)
+
+
+def read_image(path, nvox: int) -> np.ndarray:
+    out = np.empty(nvox, np.float32)
+    _ck(lib().gf_read_image(str(path).encode(), ctypes.c_int64(nvox), _ptr(out)))
+    return out
+
+
+def gpu_available() -> bool:
+    """True when a device of this library's architecture is present."""
+    try:
+        g = Geometry(16, 15, 17, 8, 3, 5, 1.6, 20.721975, 12.5)
+        Context(g).close()
+        return True
+    except (GfError, ImportError, OSError):
+        return False
+
+
+os.environ.setdefault("CUDA_MODULE_LOADING", "LAZY")

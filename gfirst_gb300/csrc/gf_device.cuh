@@ -1,0 +1,38 @@
+// gf_device.cuh -- device-side geometry and helpers shared by the kernels.
+//
+// Rounding: where a kernel must agree bit for bit with the reference's
+// expression (coordinates, the image-update chain) it uses the explicit
+// round-to-nearest intrinsics, so nvcc cannot fuse a multiply and an add the
+// source writes as two operations.  Interpolation is lerp(a,b,w) =
+// fma(w, b-a, a), the rule the CPU oracle uses for the texture unit.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gf {
+
+struct DevSeg {
+  int zmin, nplanes, acc, blk;
+  float dz, fz;
+  int pad0, pad1;
+};
+
+// Geometry passed by value to every kernel.
+struct DevGeom {
+  int res, nzs, nrad, nang, nseg, nzp;
+  int P, PP, PS, nsub;
+  float radm, resm, fx_fp, fx_bp;
+  int lam0, lam1;
+  const DevSeg* seg;    // nseg entries
+  const float2* trig;   // per angle (sin, cos)
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ float lerp_rn(float a, float b, float w) { return __fmaf_rn(w, __fsub_rn(b, a), a); }
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
+
+// Angle index of the l-th angle of subset s.
+__device__ __forceinline__ int subset_angle(const DevGeom& g, int s, int l) { return s + l * g.nsub; }
+#endif
+
+}  // namespace gf

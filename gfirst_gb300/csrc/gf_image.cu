@@ -1,0 +1,330 @@
+// gf_image.cu -- image-domain kernels on z-fast volumes [RES][RES][NZP].
+//
+// The update chain of GFIRST.cu:482-502 (divVxVGPU, convolutionXY,
+// gaussian_filterZ, multiply, edge-slice copy), the forward PSF
+// (GFIRST.cu:324-340), the joint bilateral filter (GFIRST_GPU_Kernels.cu:
+// 508-539) and layout conversions.  All of these are HBM-bound except the
+// bilateral filter; they keep the reference's operation order with explicit
+// round-to-nearest arithmetic so their results equal the reference's.
+#include "gf_kernels.h"
+
+namespace gf {
+
+// ---- separable XY Gaussian, GFIRST_GPU_Kernels.cu:332-358 -----------------
+// CTA: 8x8 columns x 32 slices.  The y pass is zero-padded; the x pass runs
+// only for 3 < x < RES-4 and border columns output the raw input.  With DIV
+// the input is the update ratio numer/denom (1 where denom < 0.001,
+// divVxVGPU, GFIRST_GPU_Kernels.cu:173-182), computed on the fly.
+template <bool DIV>
+__global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const float* __restrict__ in,
+                                                      const float* __restrict__ den, const Taps9 G,
+                                                      float* __restrict__ out) {
+  __shared__ float S[16][16][32];
+  __shared__ float Y[8][16][32];
+  const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int x0 = blockIdx.x * 8, y0 = blockIdx.y * 8, z = blockIdx.z * 32 + lane;
+  const int RES = g.res, NZP = g.nzp;
+  for (int c = ty; c < 256; c += 8) {
+    const int yy = c >> 4, xx = c & 15;
+    const int y = y0 - 4 + yy, x = x0 - 4 + xx;
+    float v = 0.f;
+    if (y >= 0 && y < RES && x >= 0 && x < RES) {
+      const size_t o = ((size_t)y * RES + x) * NZP + z;
+      if (DIV) {
+        const float b = den[o];
+        v = (b < 0.001f) ? 1.0f : __fdiv_rn(in[o], b);
+      } else {
+        v = in[o];
+      }
+    }
+    S[yy][xx][lane] = v;
+  }
+  __syncthreads();
+#pragma unroll 4
+  for (int xx = 0; xx < 16; xx++) {
+    float acc = __fmul_rn(S[ty][xx][lane], G.c[0]);
+#pragma unroll
+    for (int k = 1; k < 9; k++) acc = __fadd_rn(acc, __fmul_rn(S[ty + k][xx][lane], G.c[k]));
+    Y[ty][xx][lane] = acc;
+  }
+  __syncthreads();
+  const int y = y0 + ty;
+  if (y >= RES) return;
+#pragma unroll
+  for (int xo = 0; xo < 8; xo++) {
+    const int x = x0 + xo;
+    if (x >= RES) break;
+    float v;
+    if (x > 3 && x < RES - 4) {
+      v = __fmul_rn(Y[ty][xo][lane], G.c[0]);
+#pragma unroll
+      for (int k = 1; k < 9; k++) v = __fadd_rn(v, __fmul_rn(Y[ty][xo + k][lane], G.c[k]));
+    } else {
+      v = S[ty + 4][xo + 4][lane];
+    }
+    out[((size_t)y * RES + x) * NZP + z] = (z < g.nzs) ? v : 0.f;
+  }
+}
+
+cudaError_t launch_conv_xy(const DevGeom& g, const float* in, const float* den, const Taps9& t, float* out,
+                           cudaStream_t st) {
+  dim3 grid((g.res + 7) / 8, (g.res + 7) / 8, g.nzp / 32);
+  if (den) conv_xy_kernel<true><<<grid, 256, 0, st>>>(g, in, den, t, out);
+  else conv_xy_kernel<false><<<grid, 256, 0, st>>>(g, in, nullptr, t, out);
+  return cudaGetLastError();
+}
+
+// ---- axial filter, gaussian_filterZ (GFIRST_CPU_Kernels.cpp:165-187) -------
+// Its loop counter is incremented before use, so loop position (K, y, x)
+// writes voxel (K, y, x)+1: voxel (z, y, x) takes the rule of slice z, except
+// column (y=0, x=0), which takes the rule of slice z-1; reads past the last
+// slice are 0.  The rule is applied centred on the voxel itself.
+__device__ __forceinline__ float zrule(const float* c, int ze, int K, int NZS, const Taps5 g) {
+  auto in = [&](int zz) { return (zz >= 0 && zz < NZS) ? c[zz] : 0.f; };
+  if (K == 0) return __fadd_rn(__fmul_rn(0.5f, in(ze)), __fmul_rn(0.5f, in(ze + 1)));
+  if (K == NZS - 1) return __fadd_rn(__fmul_rn(0.5f, in(ze - 1)), __fmul_rn(0.5f, in(ze)));
+  if (K == 1 || K == NZS - 2)
+    return __fadd_rn(__fadd_rn(__fmul_rn(0.333f, in(ze - 1)), __fmul_rn(0.333f, in(ze))), __fmul_rn(0.333f, in(ze + 1)));
+  float v = __fmul_rn(g.c[0], in(ze - 2));
+  v = __fadd_rn(v, __fmul_rn(g.c[1], in(ze - 1)));
+  v = __fadd_rn(v, __fmul_rn(g.c[2], in(ze)));
+  v = __fadd_rn(v, __fmul_rn(g.c[3], in(ze + 1)));
+  v = __fadd_rn(v, __fmul_rn(g.c[4], in(ze + 2)));
+  return v;
+}
+
+// img_out = img_in * factor, then slice 0 <- slice 1 and slice NZS-1 <-
+// slice NZS-2 (GFIRST.cu:492-496).  Voxel 0's factor (DENOM[0] in the
+// reference) only reaches slice 0, which the edge copy overwrites.
+__global__ void __launch_bounds__(256) zfilter_update_kernel(const DevGeom g, const float* __restrict__ C,
+                                                             const float* __restrict__ img_in, const Taps5 t5,
+                                                             float* __restrict__ img_out) {
+  const int lane = threadIdx.x & 31;
+  const int colidx = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int z = blockIdx.y * 32 + lane;
+  if (colidx >= g.res * g.res) return;
+  const size_t cb = (size_t)colidx * g.nzp;
+  const int NZS = g.nzs;
+  if (z >= NZS) {
+    img_out[cb + z] = 0.f;
+    return;
+  }
+  const int ze = (z == 0) ? 1 : (z == NZS - 1 ? NZS - 2 : z);
+  const int K = (colidx == 0) ? ze - 1 : ze;
+  const float f = zrule(C + cb, ze, K, NZS, t5);
+  img_out[cb + z] = __fmul_rn(img_in[cb + ze], f);
+}
+
+cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const float* img_in, const Taps5& t5,
+                                  float* img_out, cudaStream_t st) {
+  dim3 grid((g.res * g.res + 7) / 8, g.nzp / 32);
+  zfilter_update_kernel<<<grid, 256, 0, st>>>(g, C, img_in, t5, img_out);
+  return cudaGetLastError();
+}
+
+// The axial filter on its own (voxel 0 keeps the value already in `out`).
+__global__ void __launch_bounds__(256) zfilter_kernel(const DevGeom g, const float* __restrict__ C, const Taps5 t5,
+                                                      float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int colidx = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int z = blockIdx.y * 32 + lane;
+  if (colidx >= g.res * g.res || z >= g.nzs) return;
+  if (colidx == 0 && z == 0) return;
+  const size_t cb = (size_t)colidx * g.nzp;
+  const int K = (colidx == 0) ? z - 1 : z;
+  out[cb + z] = zrule(C + cb, z, K, g.nzs, t5);
+}
+
+cudaError_t launch_zfilter(const DevGeom& g, const float* C, const Taps5& t5, float* out, cudaStream_t st) {
+  dim3 grid((g.res * g.res + 7) / 8, g.nzp / 32);
+  zfilter_kernel<<<grid, 256, 0, st>>>(g, C, t5, out);
+  return cudaGetLastError();
+}
+
+// ---- layout conversion ------------------------------------------------------
+// file [NZS][RES][RES] -> z-fast [RES][RES][NZP], padding slices set to 0.
+__global__ void __launch_bounds__(256) file_to_zfast_kernel(const DevGeom g, const float* __restrict__ in,
+                                                            float* __restrict__ out) {
+  __shared__ float T[32][33];
+  const int x0 = blockIdx.x * 32, y = blockIdx.y, z0 = blockIdx.z * 32;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int RES = g.res;
+  for (int j = w; j < 32; j += 8) {
+    const int z = z0 + j, x = x0 + lane;
+    T[j][lane] = (z < g.nzs && x < RES) ? in[((size_t)z * RES + y) * RES + x] : 0.f;
+  }
+  __syncthreads();
+  for (int i = w; i < 32; i += 8) {
+    const int x = x0 + i;
+    if (x < RES) out[((size_t)y * RES + x) * g.nzp + z0 + lane] = T[lane][i];
+  }
+}
+
+cudaError_t launch_file_to_zfast(const DevGeom& g, const float* in, float* out, cudaStream_t st) {
+  dim3 grid((g.res + 31) / 32, g.res, g.nzp / 32);
+  file_to_zfast_kernel<<<grid, 256, 0, st>>>(g, in, out);
+  return cudaGetLastError();
+}
+
+// z-fast -> file layout; with mask, the output scaling and the radius mask of
+// GFIRST.cu:532-549.
+__global__ void __launch_bounds__(256) zfast_to_file_kernel(const DevGeom g, const float* __restrict__ in,
+                                                            float scale, int mask, float* __restrict__ out) {
+  __shared__ float T[32][33];
+  const int x0 = blockIdx.x * 32, y = blockIdx.y, z0 = blockIdx.z * 32;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int RES = g.res;
+  for (int i = w; i < 32; i += 8) {
+    const int x = x0 + i;
+    T[i][lane] = (x < RES) ? in[((size_t)y * RES + x) * g.nzp + z0 + lane] : 0.f;
+  }
+  __syncthreads();
+  const int RESM = RES / 2;
+  for (int j = w; j < 32; j += 8) {
+    const int z = z0 + j, x = x0 + lane;
+    if (z >= g.nzs || x >= RES) continue;
+    float v = T[lane][j];
+    if (mask) {
+      const float dist = (float)((x - RESM) * (x - RESM) + (y - RESM) * (y - RESM) - (RESM - 1) * (RESM - 1));
+      v = (dist > 0.f) ? 0.f : __fmul_rn(v, scale);
+    }
+    out[((size_t)z * RES + y) * RES + x] = v;
+  }
+}
+
+cudaError_t launch_zfast_to_file(const DevGeom& g, const float* in, float scale, int mask, float* out,
+                                 cudaStream_t st) {
+  dim3 grid((g.res + 31) / 32, g.res, g.nzp / 32);
+  zfast_to_file_kernel<<<grid, 256, 0, st>>>(g, in, scale, mask, out);
+  return cudaGetLastError();
+}
+
+// CreateInitialCylinder, GFIRST_CPU_Kernels.cpp:35-56, z-fast.
+__global__ void cylinder_kernel(const DevGeom g, float val, float* out) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t n = (size_t)g.res * g.res * g.nzp;
+  if (i >= n) return;
+  const int z = (int)(i % g.nzp);
+  const int colidx = (int)(i / g.nzp);
+  const int y = colidx / g.res, x = colidx - y * g.res;
+  const int h = g.res / 2;
+  const long long r2 = (long long)(x - h) * (x - h) + (long long)(y - h) * (y - h);
+  out[i] = (z < g.nzs && r2 <= (long long)h * h) ? val : 0.f;
+}
+
+cudaError_t launch_cylinder(const DevGeom& g, float val, float* out, cudaStream_t st) {
+  const size_t n = (size_t)g.res * g.res * g.nzp;
+  cylinder_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, val, out);
+  return cudaGetLastError();
+}
+
+// max(0, max over the image), GFIRST.cu:515, 521.  d_max must hold 0 before.
+__global__ void max_nonneg_kernel(const DevGeom g, const float* __restrict__ img, float* d_max) {
+  const size_t n = (size_t)g.res * g.res * g.nzp;
+  float m = 0.f;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float v = img[i];
+    if (v > m) m = v;
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(reinterpret_cast<int*>(d_max), __float_as_int(m));
+}
+
+cudaError_t launch_max_nonneg(const DevGeom& g, const float* img, float* d_max, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(d_max, 0, sizeof(float), st);
+  if (e != cudaSuccess) return e;
+  max_nonneg_kernel<<<304, 256, 0, st>>>(g, img, d_max);
+  return cudaGetLastError();
+}
+
+// ---- joint bilateral filter, GFIRST_GPU_Kernels.cu:508-539 ---------------
+// CTA: 4x4 columns x 32 slices, reference and input staged with a halo of 4.
+// Voxels with a coordinate below r give 0 (the reference's unsigned window
+// start wraps and its loops run zero times).  Spatial weights come from a
+// table computed on the host exactly as the reference computes them
+// (double exp, stored as float); the intensity weight uses __expf in FP32
+// (the reference evaluates it in double) and the intensity difference is
+// scaled by 1/max_ref.
+constexpr int BL_T = 4, BL_H = 4;
+__global__ void __launch_bounds__(512) bilateral_kernel(const DevGeom g, const float* __restrict__ in,
+                                                        const float* __restrict__ ref,
+                                                        const float* __restrict__ d_max_ref, float max_ref_host,
+                                                        int r, float neg_inv_ci, const float* __restrict__ gtab,
+                                                        float* __restrict__ out) {
+  constexpr int W = BL_T + 2 * BL_H;  // 12 columns
+  constexpr int ZW = 32 + 2 * BL_H;   // 40 slices
+  __shared__ float Sr[W][W][ZW + 1];
+  __shared__ float Si[W][W][ZW + 1];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int x0 = blockIdx.x * BL_T, y0 = blockIdx.y * BL_T, z0 = blockIdx.z * 32;
+  const int RES = g.res, NZS = g.nzs, NZP = g.nzp;
+  for (int idx = threadIdx.x; idx < W * W * ZW; idx += blockDim.x) {
+    const int zz = idx % ZW, c = idx / ZW;
+    const int yy = c / W, xx = c % W;
+    const int y = y0 - BL_H + yy, x = x0 - BL_H + xx, z = z0 - BL_H + zz;
+    float vr = 0.f, vi = 0.f;
+    if (y >= 0 && y < RES && x >= 0 && x < RES && z >= 0 && z < NZS) {
+      const size_t o = ((size_t)y * RES + x) * NZP + z;
+      vr = ref[o];
+      vi = in[o];
+    }
+    Sr[yy][xx][zz] = vr;
+    Si[yy][xx][zz] = vi;
+  }
+  __syncthreads();
+  const int ty = wid >> 2, tx = wid & 3;
+  const int y = y0 + ty, x = x0 + tx, z = z0 + lane;
+  if (y >= RES || x >= RES) return;
+  const float max_ref = d_max_ref ? *d_max_ref : max_ref_host;
+  const float rinv = 1.0f / max_ref;
+  float res = 0.f;
+  if (z < NZS && x >= r && y >= r && z >= r) {
+    const float ref0 = Sr[ty + BL_H][tx + BL_H][lane + BL_H];
+    float norm = 0.f, sum = 0.f;
+    for (int dz = -r; dz <= r; dz++) {
+      if (z + dz >= NZS) break;
+      for (int dy = -r; dy <= r; dy++) {
+        if (y + dy >= RES) break;
+        const float* rr = &Sr[ty + BL_H + dy][tx + BL_H][lane + BL_H + dz];
+        const float* ii = &Si[ty + BL_H + dy][tx + BL_H][lane + BL_H + dz];
+        const float* gw = gtab + ((dz + 4) * 9 + (dy + 4)) * 9 + 4;
+        for (int dx = -r; dx <= r; dx++) {
+          if (x + dx >= RES) break;
+          const float d = __fmul_rn(__fsub_rn(rr[dx * (ZW + 1)], ref0), rinv);
+          const float h = __expf(__fmul_rn(__fmul_rn(d, d), neg_inv_ci));
+          const float w = __fmul_rn(h, __ldg(gw + dx));
+          norm = __fadd_rn(norm, w);
+          sum = __fadd_rn(sum, __fmul_rn(w, ii[dx * (ZW + 1)]));
+        }
+      }
+    }
+    res = ((double)norm > 1e-8) ? __fdiv_rn(sum, norm) : 0.f;
+  }
+  out[((size_t)y * RES + x) * NZP + z] = (z < NZS) ? res : 0.f;
+}
+
+cudaError_t launch_bilateral(const DevGeom& g, const float* in, const float* ref, const float* d_max_ref,
+                             float max_ref, int r, float sigmai, const float* gtab, float* out, cudaStream_t st) {
+  if (r < 0 || r > BL_H) return cudaErrorInvalidValue;
+  const double ci = (2.0 * (double)sigmai) * (2.0 * (double)sigmai);
+  const float neg_inv_ci = (float)(-1.0 / ci);
+  dim3 grid((g.res + BL_T - 1) / BL_T, (g.res + BL_T - 1) / BL_T, g.nzp / 32);
+  bilateral_kernel<<<grid, 512, 0, st>>>(g, in, ref, d_max_ref, max_ref, r, neg_inv_ci, gtab, out);
+  return cudaGetLastError();
+}
+
+// img2 = (1.0 - 0.1f)*img2 + 0.1f*filtered, GFIRST.cu:524 (double, as there).
+__global__ void blend_kernel(size_t n, float* img2, const float* __restrict__ filt) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float fc = 0.1f;
+  img2[i] = (float)(__dadd_rn(__dmul_rn(1.0 - (double)fc, (double)img2[i]), (double)__fmul_rn(fc, filt[i])));
+}
+
+cudaError_t launch_blend(const DevGeom& g, float* img2, const float* filt, cudaStream_t st) {
+  const size_t n = (size_t)g.res * g.res * g.nzp;
+  blend_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, img2, filt);
+  return cudaGetLastError();
+}
+
+}  // namespace gf

@@ -1,0 +1,107 @@
+// gf_internal.h -- host-side context and reconstruction objects behind the C-ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gfirst.h"
+#include "gf_kernels.h"
+#include "gf_plan.h"
+
+namespace gf {
+
+gf_status set_error(gf_status st, const std::string& msg);
+gf_status cuda_error(cudaError_t e, const char* what);
+
+#define GF_CK(x)                                                \
+  do {                                                          \
+    cudaError_t e__ = (x);                                      \
+    if (e__ != cudaSuccess) return ::gf::cuda_error(e__, #x);   \
+  } while (0)
+
+#define GF_TRY(x)                         \
+  do {                                    \
+    gf_status s__ = (x);                  \
+    if (s__ != GF_OK) return s__;         \
+  } while (0)
+
+Taps9 gauss9(float psf);   // calcGaussianCoefficients, GFIRST_GPU_Kernels.cu:322-330
+Taps5 gauss5();            // gaussian_filterZ's taps, GFIRST_CPU_Kernels.cpp:169-173
+std::vector<float> bilateral_table(float sigma3d);  // 9x9x9 spatial weights
+
+// Device buffer owned by a context or reconstruction.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace gf
+
+struct gf_ctx {
+  gf::Plan plan;
+  gf::FpSchedule fps;
+  gf::DevGeom dg{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::vector<gf::DevBuf> owned;  // freed on destroy
+  gf::DevSeg* d_seg = nullptr;
+  float2* d_trig = nullptr;
+  int2* d_rowmap = nullptr;
+  int4* d_runs = nullptr;
+  float* d_gtab = nullptr;
+  float gtab_sigma = -1.f;
+  // scratch of the operator entry points, allocated on first use
+  float* s_img = nullptr;
+  float* s_img2 = nullptr;
+  float* s_numer = nullptr;
+  float* s_denom = nullptr;
+  float2* s_cc = nullptr;
+
+  gf_status alloc(size_t bytes, void** p);
+  template <class T> gf_status alloc_t(size_t n, T** p) {
+    return alloc(n * sizeof(T), reinterpret_cast<void**>(p));
+  }
+  gf_status ensure_scratch();
+  gf_status ensure_gtab(float sigma3d);
+  gf::FpArgs fp_args(int subset, const float* img_zfast) const;
+};
+
+struct gf_recon {
+  gf_ctx* ctx = nullptr;
+  gf_recon_params p{};
+  int ntypes = 1;
+  bool loaded = false;
+  std::vector<gf::DevBuf> owned;
+  float* img[2] = {nullptr, nullptr};  // z-fast images (doubles, triples)
+  float* img_alt = nullptr;            // update output, swapped with img[t]
+  float* psf = nullptr;
+  float* numer = nullptr;
+  float* denom = nullptr;
+  float* ctmp = nullptr;
+  float* filt = nullptr;
+  float2* corrcal = nullptr;
+  float2* dbg[2] = {nullptr, nullptr};
+  float* cal = nullptr;
+  float* proj_ref = nullptr;
+  float* proj_t = nullptr;  // triples projection, file layout (VLOR split weights)
+  int32_t* events = nullptr;
+  int64_t nev = 0;
+  float* blankt = nullptr;
+  float* datos_v = nullptr;
+  float* d_max = nullptr;
+  gf::Taps9 g_fw{}, g_bw{};
+  gf::Taps5 g5{};
+  int iters_done = 0;
+  int64_t subs_done = 0;
+  int cur_type = 0, cur_sub = 0;
+
+  gf_status alloc(size_t bytes, void** p);
+  template <class T> gf_status alloc_t(size_t n, T** q) {
+    return alloc(n * sizeof(T), reinterpret_cast<void**>(q));
+  }
+  gf_status subiteration(int type, int subset);
+  gf_status project_all(const float* img_zfast, float* proj_full);
+};

@@ -1,0 +1,76 @@
+// gf_kernels.h -- host-callable launchers of the sm_103a kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "gf_device.cuh"
+#include "gf_plan.h"
+
+namespace gf {
+
+struct Taps9 { float c[9]; };
+struct Taps5 { float c[5]; };
+
+// ---- forward projector (gf_fp.cu) ----
+struct FpArgs {
+  DevGeom g;
+  int subset;
+  const float* img;        // z-fast image (after the forward PSF)
+  const int4* runs;        // FpSchedule::runs as (seg, p0, n, pad)
+  int nruns, padl, cw, lc;
+  const float2* dbg;       // subset layout (data*RES, max(bg*RES,0)); with corrcal
+  const float* cal;        // subset layout normalization mask; with corrcal
+  float2* corrcal;         // subset layout (corr, calib) output, or null
+  float* proj_full;        // file-layout projection output, or null
+};
+cudaError_t launch_fp(const FpArgs& a, const FpSchedule& s, cudaStream_t st);
+
+// ---- back projector (gf_bp.cu) ----
+struct BpArgs {
+  DevGeom g;
+  int subset, na;          // na: angles in this subset
+  const float2* corrcal;   // subset layout (corr, calib)
+  float* numer;            // z-fast
+  float* denom;            // z-fast
+};
+cudaError_t launch_bp(const BpArgs& a, cudaStream_t st);
+
+// ---- image kernels (gf_image.cu) ----
+// out = XY PSF of `in`; with `den` the input is the update ratio in/den.
+cudaError_t launch_conv_xy(const DevGeom& g, const float* in, const float* den, const Taps9& t, float* out,
+                           cudaStream_t st);
+// img_out = img_in * axial_filter(C) with the edge-slice copy.
+cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const float* img_in, const Taps5& t5,
+                                  float* img_out, cudaStream_t st);
+// Axial filter alone, z-fast in/out (voxel 0 keeps out's value).
+cudaError_t launch_zfilter(const DevGeom& g, const float* C, const Taps5& t5, float* out, cudaStream_t st);
+cudaError_t launch_file_to_zfast(const DevGeom& g, const float* in, float* out, cudaStream_t st);
+cudaError_t launch_zfast_to_file(const DevGeom& g, const float* in, float scale, int mask, float* out,
+                                 cudaStream_t st);
+cudaError_t launch_cylinder(const DevGeom& g, float val, float* out, cudaStream_t st);
+cudaError_t launch_max_nonneg(const DevGeom& g, const float* img, float* d_max, cudaStream_t st);
+cudaError_t launch_bilateral(const DevGeom& g, const float* in, const float* ref, const float* d_max_ref,
+                             float max_ref, int r, float sigmai, const float* gtab, float* out, cudaStream_t st);
+cudaError_t launch_blend(const DevGeom& g, float* img2, const float* filt, cudaStream_t st);
+
+// ---- sinogram kernels (gf_sino.cu) ----
+// rowmap[row'] = (segment, plane) of a padded row, (-1,-1) for a pad row.
+cudaError_t launch_build_dbg(const DevGeom& g, const int2* rowmap, const float* sino2, float2* dbg,
+                             cudaStream_t st);
+cudaError_t launch_build_cal(const DevGeom& g, const int2* rowmap, const float* proj_ref, const float* norm,
+                             float* cal, cudaStream_t st);
+cudaError_t launch_corrcal_from_file(const DevGeom& g, const int2* rowmap, int subset, int na, const float* corr,
+                                     const float* calib, float2* corrcal, cudaStream_t st);
+cudaError_t launch_ratio_gather(const DevGeom& g, const int2* rowmap, int subset, int na, const float* proj_full,
+                                const float* datos_v, const float2* dbg_t, const float* cal, float2* corrcal,
+                                cudaStream_t st);
+cudaError_t launch_ratio_file(const DevGeom& g, int subset, const float* proj, const float* data, const float* bg,
+                              float* corr, cudaStream_t st);
+cudaError_t launch_norm_mask(const DevGeom& g, const float* proj_blank, const float* blank, float* calib,
+                             cudaStream_t st);
+cudaError_t launch_vlor_count(const DevGeom& g, const int32_t* ev, long long nev, float* cnt, cudaStream_t st);
+cudaError_t launch_blankt(const DevGeom& g, const float* cnt, const float* tsino_raw, float* blankt,
+                          cudaStream_t st);
+cudaError_t launch_vlor_split(const DevGeom& g, const int32_t* ev, long long nev, const float* proj,
+                              const float* blankt, float* out, cudaStream_t st);
+
+}  // namespace gf

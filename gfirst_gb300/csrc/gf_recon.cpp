@@ -1,0 +1,287 @@
+// gf_recon.cpp -- one reconstruction of a CLI mode, resident on the device.
+//
+// Replaces osem3d() (GFIRST.cu:44-575).  The reference keeps its images on
+// the host and crosses to the device once per view; here every array stays
+// in HBM for the whole reconstruction and a sub-iteration is a fixed chain
+// of kernels on one stream:
+//   psf    = XY PSF of the current image                      (GFIRST.cu:324-340)
+//   FP     = forward projection + ratio -> (corr, calib)       (GFIRST.cu:346-430)
+//            [VLOR triples: FP -> split -> ratio, GFIRST.cu:373-430]
+//   BP     = back projection -> NUMER, DENOM                   (GFIRST.cu:436-469)
+//   update = ratio, XY PSF, axial filter, multiply, edges      (GFIRST.cu:482-502)
+//   [triples, once per iteration: joint bilateral filter + blend, GFIRST.cu:510-526]
+// Subset s holds the angles t with t % nsub == s; sub-iterations run
+// iteration -> type (doubles, triples) -> subset.  With nsub = 1 this is the
+// reference's loop.  The joint filter runs after the triples type's last
+// subset, i.e. once per iteration as in the reference.
+#include <cstring>
+
+#include "gf_internal.h"
+
+using namespace gf;
+
+gf_status gf_recon::alloc(size_t bytes, void** q) {
+  *q = nullptr;
+  cudaError_t e = cudaMalloc(q, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_error(e, "cudaMalloc (reconstruction)");
+  }
+  owned.push_back(DevBuf{*q, bytes});
+  return GF_OK;
+}
+
+gf_status gf_recon::project_all(const float* img_zfast, float* proj_full) {
+  for (int s = 0; s < ctx->plan.nsub; s++) {
+    FpArgs a = ctx->fp_args(s, img_zfast);
+    a.proj_full = proj_full;
+    GF_CK(launch_fp(a, ctx->fps, ctx->stream));
+  }
+  return GF_OK;
+}
+
+gf_status gf_recon::subiteration(int t, int s) {
+  gf_ctx* c = ctx;
+  const Plan& pl = c->plan;
+  cudaStream_t st = c->stream;
+  const int na = pl.sub_nang[s];
+  const int64_t off = pl.sub_off[s];
+  GF_CK(launch_conv_xy(c->dg, img[t], nullptr, g_fw, psf, st));
+  FpArgs a = c->fp_args(s, psf);
+  if (p.mode == 3 && t == 1) {
+    a.proj_full = proj_t;
+    GF_CK(launch_fp(a, c->fps, st));
+    GF_CK(cudaMemsetAsync(datos_v, 0, (size_t)pl.ndata * sizeof(float), st));
+    GF_CK(launch_vlor_split(c->dg, events, nev, proj_t, blankt, datos_v, st));
+    GF_CK(launch_ratio_gather(c->dg, c->d_rowmap, s, na, proj_t, datos_v, dbg[1] + off, cal + off, corrcal, st));
+  } else {
+    a.dbg = dbg[t] + off;
+    a.cal = cal + off;
+    a.corrcal = corrcal;
+    GF_CK(launch_fp(a, c->fps, st));
+  }
+  BpArgs b{c->dg, s, na, corrcal, numer, denom};
+  GF_CK(launch_bp(b, st));
+  GF_CK(launch_conv_xy(c->dg, numer, denom, g_bw, ctmp, st));
+  GF_CK(launch_zfilter_update(c->dg, ctmp, img[t], g5, img_alt, st));
+  float* tmp = img[t];
+  img[t] = img_alt;
+  img_alt = tmp;
+  if (t == 1 && s == pl.nsub - 1) {
+    // GFIRST.cu:512-524: r=4, sigma3D=0.75, sigmaI=0.025, max_ref over the doubles image
+    GF_CK(launch_max_nonneg(c->dg, img[0], d_max, st));
+    GF_CK(launch_bilateral(c->dg, img[1], img[0], d_max, 0.f, 4, 0.025f, c->d_gtab, filt, st));
+    GF_CK(launch_blend(c->dg, img[1], filt, st));
+  }
+  return GF_OK;
+}
+
+extern "C" {
+
+gf_status gf_recon_defaults(int32_t mode, gf_recon_params* out) {
+  if (!out) return set_error(GF_ERR_ARG, "null output");
+  if (mode < 0 || mode > 3) return set_error(GF_ERR_ARG, "mode must be 0..3");
+  // GFIRST.h:21-30
+  out->mode = mode;
+  out->niter = 60;
+  out->psf_fw = 1.5f;
+  out->psf_bw = 1.5f;
+  out->scale_d = (float)(3.70e-4 * 162.0);
+  out->scale_t = (float)(3.70e-4 * 162.0);
+  return GF_OK;
+}
+
+gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out) {
+  if (!c || !prm || !out) return set_error(GF_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (prm->mode < 0 || prm->mode > 3) return set_error(GF_ERR_ARG, "mode must be 0..3");
+  if (prm->niter < 0) return set_error(GF_ERR_ARG, "niter must be >= 0");
+  GF_CK(cudaSetDevice(c->device));
+  gf_recon* r = new gf_recon();
+  r->ctx = c;
+  r->p = *prm;
+  r->ntypes = prm->mode == 0 ? 0 : (prm->mode == 1 ? 1 : 2);
+  const Plan& pl = c->plan;
+  auto fail = [&](gf_status st) {
+    gf_recon_destroy(r);
+    return st;
+  };
+  gf_status st;
+#define ALLOC(ptr, n) \
+  if ((st = r->alloc_t((size_t)(n), &(ptr))) != GF_OK) return fail(st)
+  ALLOC(r->img[0], pl.nvoxp);
+  ALLOC(r->proj_ref, pl.ndata);
+  if (prm->mode >= 1) {
+    ALLOC(r->img[1], pl.nvoxp);
+    ALLOC(r->img_alt, pl.nvoxp);
+    ALLOC(r->psf, pl.nvoxp);
+    ALLOC(r->numer, pl.nvoxp);
+    ALLOC(r->denom, pl.nvoxp);
+    ALLOC(r->ctmp, pl.nvoxp);
+    ALLOC(r->corrcal, (size_t)pl.amax * pl.g.nrad * pl.PS);
+    ALLOC(r->dbg[0], pl.all_elems());
+    ALLOC(r->cal, pl.all_elems());
+  }
+  if (prm->mode >= 2) {
+    ALLOC(r->dbg[1], pl.all_elems());
+    ALLOC(r->filt, pl.nvoxp);
+    ALLOC(r->d_max, 1);
+    if ((st = c->ensure_gtab(0.75f)) != GF_OK) return fail(st);
+  }
+  if (prm->mode == 3) {
+    ALLOC(r->proj_t, pl.ndata);
+    ALLOC(r->blankt, pl.ndata);
+    ALLOC(r->datos_v, pl.ndata);
+  }
+#undef ALLOC
+  r->g_fw = gauss9(prm->psf_fw);
+  r->g_bw = gauss9(prm->psf_bw);
+  r->g5 = gauss5();
+  *out = r;
+  return GF_OK;
+}
+
+void gf_recon_destroy(gf_recon* r) {
+  if (!r) return;
+  if (r->ctx) cudaStreamSynchronize(r->ctx->stream);
+  for (auto& b : r->owned) cudaFree(b.p);
+  delete r;
+}
+
+gf_status gf_recon_load(gf_recon* r, const float* h_image, const float* h_dsino, const float* h_tsino,
+                        const float* h_norm, const int32_t* h_events, int64_t nevents) {
+  if (!r) return set_error(GF_ERR_ARG, "null reconstruction");
+  gf_ctx* c = r->ctx;
+  const Plan& pl = c->plan;
+  cudaStream_t st = c->stream;
+  const int mode = r->p.mode;
+  if (mode == 0 && !h_image) return set_error(GF_ERR_ARG, "mode 0 needs an image");
+  if (mode >= 1 && (!h_dsino || !h_norm)) return set_error(GF_ERR_ARG, "modes 1-3 need a sinogram and a normalization");
+  if (mode >= 2 && !h_tsino) return set_error(GF_ERR_ARG, "modes 2-3 need a triples sinogram");
+  if (mode == 3 && (nevents < 0 || (nevents > 0 && !h_events))) return set_error(GF_ERR_ARG, "mode 3 needs VLOR events");
+  GF_CK(cudaSetDevice(c->device));
+  // staging buffer for the host inputs, freed at the end of the load
+  float* stage = nullptr;
+  size_t stage_n = (size_t)2 * pl.ndata + (size_t)pl.ndata;
+  if (mode == 0) stage_n = pl.nvox;
+  GF_CK(cudaMalloc(&stage, stage_n * sizeof(float)));
+  auto done = [&](gf_status s) {
+    cudaStreamSynchronize(st);
+    cudaFree(stage);
+    return s;
+  };
+  auto ck = [&](cudaError_t e, const char* w) { return e == cudaSuccess ? GF_OK : cuda_error(e, w); };
+  gf_status s;
+  if (mode == 0) {
+    if ((s = ck(cudaMemcpyAsync(stage, h_image, pl.nvox * sizeof(float), cudaMemcpyHostToDevice, st), "upload image")) != GF_OK) return done(s);
+    if ((s = ck(launch_file_to_zfast(c->dg, stage, r->img[0], st), "layout")) != GF_OK) return done(s);
+    if ((s = r->project_all(r->img[0], r->proj_ref)) != GF_OK) return done(s);
+    r->loaded = true;
+    return done(GF_OK);
+  }
+  // STEP 1: projection of a unit cylinder -> proj_ref (GFIRST.cu:151-184)
+  if ((s = ck(launch_cylinder(c->dg, 1.0f, r->img[0], st), "cylinder")) != GF_OK) return done(s);
+  if ((s = r->project_all(r->img[0], r->proj_ref)) != GF_OK) return done(s);
+  // STEP 2: data (GFIRST.cu:207-260)
+  float* s2 = stage;                      // 2*NDATA
+  float* sn = stage + 2 * pl.ndata;       // NDATA
+  if ((s = ck(cudaMemcpyAsync(s2, h_dsino, 2 * pl.ndata * sizeof(float), cudaMemcpyHostToDevice, st), "upload sinogram")) != GF_OK) return done(s);
+  if ((s = ck(launch_build_dbg(c->dg, c->d_rowmap, s2, r->dbg[0], st), "build data")) != GF_OK) return done(s);
+  if ((s = ck(cudaMemcpyAsync(sn, h_norm, pl.ndata * sizeof(float), cudaMemcpyHostToDevice, st), "upload norm")) != GF_OK) return done(s);
+  if ((s = ck(launch_build_cal(c->dg, c->d_rowmap, r->proj_ref, sn, r->cal, st), "build mask")) != GF_OK) return done(s);
+  if (mode >= 2) {
+    if ((s = ck(cudaMemcpyAsync(s2, h_tsino, 2 * pl.ndata * sizeof(float), cudaMemcpyHostToDevice, st), "upload triples")) != GF_OK) return done(s);
+    if ((s = ck(launch_build_dbg(c->dg, c->d_rowmap, s2, r->dbg[1], st), "build triples")) != GF_OK) return done(s);
+  }
+  if (mode == 3) {
+    r->nev = nevents;
+    if (nevents > 0) {
+      if ((s = r->alloc_t((size_t)nevents * 2, &r->events)) != GF_OK) return done(s);
+      if ((s = ck(cudaMemcpyAsync(r->events, h_events, (size_t)nevents * 2 * sizeof(int32_t), cudaMemcpyHostToDevice, st), "upload events")) != GF_OK) return done(s);
+    }
+    // counts in datos_v (scratch for now), then BLANKT (GFIRST.cu:229-247)
+    if ((s = ck(cudaMemsetAsync(r->datos_v, 0, pl.ndata * sizeof(float), st), "memset")) != GF_OK) return done(s);
+    if ((s = ck(launch_vlor_count(c->dg, r->events, nevents, r->datos_v, st), "vlor count")) != GF_OK) return done(s);
+    if ((s = ck(launch_blankt(c->dg, r->datos_v, s2, r->blankt, st), "blankt")) != GF_OK) return done(s);
+  }
+  // STEP 3: initial images (GFIRST.cu:282-288)
+  if ((s = ck(launch_cylinder(c->dg, 1.0f, r->img[0], st), "cylinder")) != GF_OK) return done(s);
+  if ((s = ck(launch_cylinder(c->dg, mode == 1 ? 0.0f : 1.0f, r->img[1], st), "cylinder")) != GF_OK) return done(s);
+  if (mode == 3) {
+    // the triples projection that weights the VLOR split, refreshed subset by subset
+    if ((s = ck(launch_conv_xy(c->dg, r->img[1], nullptr, r->g_fw, r->psf, st), "psf")) != GF_OK) return done(s);
+    if ((s = r->project_all(r->psf, r->proj_t)) != GF_OK) return done(s);
+    if ((s = ck(cudaMemsetAsync(r->datos_v, 0, pl.ndata * sizeof(float), st), "memset")) != GF_OK) return done(s);
+  }
+  r->loaded = true;
+  r->iters_done = 0;
+  r->subs_done = 0;
+  r->cur_type = r->cur_sub = 0;
+  return done(GF_OK);
+}
+
+gf_status gf_recon_subiteration(gf_recon* r) {
+  if (!r) return set_error(GF_ERR_ARG, "null reconstruction");
+  if (!r->loaded) return set_error(GF_ERR_STATE, "gf_recon_load has not run");
+  if (r->ntypes == 0) return set_error(GF_ERR_STATE, "mode 0 has no iterations");
+  GF_TRY(r->subiteration(r->cur_type, r->cur_sub));
+  r->subs_done++;
+  if (++r->cur_sub == r->ctx->plan.nsub) {
+    r->cur_sub = 0;
+    if (++r->cur_type == r->ntypes) {
+      r->cur_type = 0;
+      r->iters_done++;
+    }
+  }
+  return GF_OK;
+}
+
+gf_status gf_recon_iterate(gf_recon* r, int32_t n) {
+  if (!r) return set_error(GF_ERR_ARG, "null reconstruction");
+  if (n < 0) return set_error(GF_ERR_ARG, "n must be >= 0");
+  if (r->ntypes == 0) return n == 0 ? GF_OK : set_error(GF_ERR_STATE, "mode 0 has no iterations");
+  const int64_t per = (int64_t)r->ntypes * r->ctx->plan.nsub;
+  for (int64_t k = 0; k < per * n; k++) GF_TRY(gf_recon_subiteration(r));
+  return GF_OK;
+}
+
+gf_status gf_recon_progress(const gf_recon* r, int32_t* it, int64_t* sub) {
+  if (!r) return set_error(GF_ERR_ARG, "null reconstruction");
+  if (it) *it = r->iters_done;
+  if (sub) *sub = r->subs_done;
+  return GF_OK;
+}
+
+gf_status gf_recon_get_image(gf_recon* r, int32_t type, int32_t scaled, float* h_out) {
+  if (!r || !h_out) return set_error(GF_ERR_ARG, "null argument");
+  if (type < 0 || type > 1 || !r->img[type]) return set_error(GF_ERR_ARG, "no such image");
+  gf_ctx* c = r->ctx;
+  const Plan& pl = c->plan;
+  float* tmp = nullptr;
+  GF_CK(cudaMalloc(&tmp, pl.nvox * sizeof(float)));
+  const float scale = type == 0 ? r->p.scale_d : r->p.scale_t;
+  cudaError_t e = launch_zfast_to_file(c->dg, r->img[type], scale, scaled ? 1 : 0, tmp, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h_out, tmp, pl.nvox * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return cuda_error(e, "get image");
+  return GF_OK;
+}
+
+gf_status gf_recon_get_proj_ref(gf_recon* r, float* h_out) {
+  if (!r || !h_out) return set_error(GF_ERR_ARG, "null argument");
+  if (!r->loaded) return set_error(GF_ERR_STATE, "gf_recon_load has not run");
+  GF_CK(cudaMemcpyAsync(h_out, r->proj_ref, r->ctx->plan.ndata * sizeof(float), cudaMemcpyDeviceToHost, r->ctx->stream));
+  GF_CK(cudaStreamSynchronize(r->ctx->stream));
+  return GF_OK;
+}
+
+gf_status gf_recon_get_sinog_vlor(gf_recon* r, float* h_out) {
+  if (!r || !h_out) return set_error(GF_ERR_ARG, "null argument");
+  if (r->p.mode != 3) return set_error(GF_ERR_STATE, "only mode 3 splits VLOR events");
+  GF_CK(cudaMemcpyAsync(h_out, r->datos_v, r->ctx->plan.ndata * sizeof(float), cudaMemcpyDeviceToHost, r->ctx->stream));
+  GF_CK(cudaStreamSynchronize(r->ctx->stream));
+  return GF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,264 @@
+// gf_sino.cu -- sinogram-domain kernels: the subset-local (radial-major,
+// padded-row) layouts the projectors use, the data/projection ratio, the
+// normalization mask and the VLOR count/split.
+//
+// Elements of a subset-layout array are indexed by
+//   (angle-in-subset tl, radial bin r, padded row p): (tl*NRAD + r)*PS + p,
+// with one array holding every subset back to back when it is static.
+#include "gf_kernels.h"
+
+namespace gf {
+
+__device__ __forceinline__ size_t file_lor(const DevGeom& g, int seg, int plane, int theta, int r) {
+  const DevSeg& sg = g.seg[seg];
+  return ((size_t)(plane - sg.zmin) + sg.acc) * ((size_t)g.nrad * g.nang) + (size_t)theta * g.nrad + r;
+}
+
+// rowmap entries: (seg, plane) for real rows; (seg, -1 - edge) for pad rows,
+// edge 0 = before the block, 1 = after; (-1, -1) past PP.
+__device__ __forceinline__ bool resolve_row(const DevGeom& g, int2 m, int* seg, int* plane) {
+  if (m.x < 0) return false;
+  *seg = m.x;
+  if (m.y >= 0) {
+    *plane = m.y;
+    return true;
+  }
+  if (m.x != 0) return false;  // oblique pad row: sentinel
+  *plane = (m.y == -1) ? 0 : g.nzs - 1;
+  return true;
+}
+
+// All-subset element index -> (subset-local angle, angle, radial, row).
+__device__ __forceinline__ void decode_all(const DevGeom& g, size_t i, int* theta, int* r, int* p) {
+  *p = (int)(i % g.PS);
+  const size_t q = i / g.PS;
+  *r = (int)(q % g.nrad);
+  const int idx = (int)(q / g.nrad);  // angle rank within the concatenated subsets
+  // subsets are stored in order; subset s holds angles s, s+nsub, ...
+  int s = 0, base = 0;
+  for (;;) {
+    const int na = (g.nang - s + g.nsub - 1) / g.nsub;
+    if (idx < base + na) {
+      *theta = s + (idx - base) * g.nsub;
+      return;
+    }
+    base += na;
+    s++;
+  }
+}
+
+// (data*RES, max(bg*RES, 0)) for every subset, from the parsed file
+// (2*NDATA floats: prompts then background).  GFIRST.cu:224-226, 423.
+__global__ void build_dbg_kernel(const DevGeom g, const int2* __restrict__ rowmap, const float* __restrict__ sino2,
+                                 float2* __restrict__ dbg, size_t n, size_t ndata) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int theta, r, p, seg, plane;
+  decode_all(g, i, &theta, &r, &p);
+  float2 v = make_float2(0.f, 0.f);
+  const int2 m = rowmap[p];
+  if (m.x >= 0 && m.y >= 0) {
+    seg = m.x;
+    plane = m.y;
+    const size_t lor = file_lor(g, seg, plane, theta, r);
+    const float res = (float)g.res;
+    const float bg = __fmul_rn(res, sino2[ndata + lor]);
+    v = make_float2(__fmul_rn(res, sino2[lor]), ((double)bg < 0.) ? 0.f : bg);
+  }
+  dbg[i] = v;
+}
+
+cudaError_t launch_build_dbg(const DevGeom& g, const int2* rowmap, const float* sino2, float2* dbg,
+                             cudaStream_t st) {
+  const size_t n = (size_t)g.nang * g.nrad * g.PS;
+  const size_t ndata = (size_t)g.P * g.nang * g.nrad;
+  build_dbg_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, rowmap, sino2, dbg, n, ndata);
+  return cudaGetLastError();
+}
+
+// Normalization mask per subset element, GFIRST.cu:447, 453-458: 1 where
+// proj_blank > 0.01 and blank > 0.01, else -1000; oblique pad rows -1000.
+__global__ void build_cal_kernel(const DevGeom g, const int2* __restrict__ rowmap, const float* __restrict__ proj_ref,
+                                 const float* __restrict__ norm, float* __restrict__ cal, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int theta, r, p, seg, plane;
+  decode_all(g, i, &theta, &r, &p);
+  float v = -1000.f;
+  if (resolve_row(g, rowmap[p], &seg, &plane)) {
+    const size_t lor = file_lor(g, seg, plane, theta, r);
+    v = ((double)proj_ref[lor] > 0.01 && (double)norm[lor] > 0.01) ? 1.0f : -1000.f;
+  }
+  cal[i] = v;
+}
+
+cudaError_t launch_build_cal(const DevGeom& g, const int2* rowmap, const float* proj_ref, const float* norm,
+                             float* cal, cudaStream_t st) {
+  const size_t n = (size_t)g.nang * g.nrad * g.PS;
+  build_cal_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, rowmap, proj_ref, norm, cal, n);
+  return cudaGetLastError();
+}
+
+__device__ __forceinline__ float ratio_rule(float proj, float data, float bg) {
+  // GFIRST.cu:423-429
+  if ((double)bg < 0.) bg = 0.f;
+  const float s = __fadd_rn(proj, bg);
+  return (s >= 0.01f) ? __fdiv_rn(data, s) : -1000.f;
+}
+
+// (corr, calib) pairs of one subset from file-layout corr and calib.
+__global__ void corrcal_from_file_kernel(const DevGeom g, const int2* __restrict__ rowmap, int subset,
+                                         const float* __restrict__ corr, const float* __restrict__ calib,
+                                         float2* __restrict__ cc, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int p = (int)(i % g.PS);
+  const size_t q = i / g.PS;
+  const int r = (int)(q % g.nrad), tl = (int)(q / g.nrad);
+  const int theta = subset_angle(g, subset, tl);
+  int seg, plane;
+  float2 v = make_float2(-1000.f, -1000.f);
+  if (resolve_row(g, rowmap[p], &seg, &plane)) {
+    const size_t lor = file_lor(g, seg, plane, theta, r);
+    v = make_float2(corr[lor], calib[lor]);
+  }
+  cc[i] = v;
+}
+
+cudaError_t launch_corrcal_from_file(const DevGeom& g, const int2* rowmap, int subset, int na, const float* corr,
+                                     const float* calib, float2* corrcal, cudaStream_t st) {
+  const size_t n = (size_t)na * g.nrad * g.PS;
+  corrcal_from_file_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, rowmap, subset, corr, calib, corrcal, n);
+  return cudaGetLastError();
+}
+
+// Ratio for the VLOR triples (GFIRST.cu:415-430 with val_dato = datos_v*RES,
+// GFIRST.cu:397, 421) written as (corr, calib) pairs of one subset.
+__global__ void ratio_gather_kernel(const DevGeom g, const int2* __restrict__ rowmap, int subset,
+                                    const float* __restrict__ proj_full, const float* __restrict__ datos_v,
+                                    const float2* __restrict__ dbg_t, const float* __restrict__ cal,
+                                    float2* __restrict__ cc, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int p = (int)(i % g.PS);
+  const size_t q = i / g.PS;
+  const int r = (int)(q % g.nrad), tl = (int)(q / g.nrad);
+  const int theta = subset_angle(g, subset, tl);
+  int seg, plane;
+  float2 v = make_float2(-1000.f, -1000.f);
+  const int2 m = rowmap[p];
+  if (resolve_row(g, m, &seg, &plane)) {
+    const size_t lor = file_lor(g, seg, plane, theta, r);
+    // the edge row's own element for segment 0's pad rows
+    const int prow = (m.y >= 0) ? p : (m.y == -1 ? p + 1 : p - 1);
+    const size_t e = i - p + prow;
+    const float data = __fmul_rn(datos_v[lor], (float)g.res);
+    v = make_float2(ratio_rule(proj_full[lor], data, dbg_t[e].y), cal[e]);
+  }
+  cc[i] = v;
+}
+
+cudaError_t launch_ratio_gather(const DevGeom& g, const int2* rowmap, int subset, int na, const float* proj_full,
+                                const float* datos_v, const float2* dbg_t, const float* cal, float2* corrcal,
+                                cudaStream_t st) {
+  const size_t n = (size_t)na * g.nrad * g.PS;
+  ratio_gather_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, rowmap, subset, proj_full, datos_v, dbg_t,
+                                                                    cal, corrcal, n);
+  return cudaGetLastError();
+}
+
+// File-layout ratio over one subset's bins (operator entry point).
+__global__ void ratio_file_kernel(const DevGeom g, int subset, const float* __restrict__ proj,
+                                  const float* __restrict__ data, const float* __restrict__ bg,
+                                  float* __restrict__ corr, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int theta = (int)((i / g.nrad) % g.nang);
+  if (theta % g.nsub != subset) return;
+  corr[i] = ratio_rule(proj[i], data[i], bg[i]);
+}
+
+cudaError_t launch_ratio_file(const DevGeom& g, int subset, const float* proj, const float* data, const float* bg,
+                              float* corr, cudaStream_t st) {
+  const size_t n = (size_t)g.P * g.nang * g.nrad;
+  ratio_file_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, subset, proj, data, bg, corr, n);
+  return cudaGetLastError();
+}
+
+__global__ void norm_mask_kernel(const float* __restrict__ pb, const float* __restrict__ b, float* __restrict__ c,
+                                 size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  c[i] = ((double)pb[i] > 0.01 && (double)b[i] > 0.01) ? 1.0f : -1000.f;
+}
+
+cudaError_t launch_norm_mask(const DevGeom& g, const float* proj_blank, const float* blank, float* calib,
+                             cudaStream_t st) {
+  const size_t n = (size_t)g.P * g.nang * g.nrad;
+  norm_mask_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(proj_blank, blank, calib, n);
+  return cudaGetLastError();
+}
+
+// ---- VLOR, GFIRST.cu:229-247, 373-389 --------------------------------------
+__device__ __forceinline__ bool vlor_bins(const int32_t* ev, long long e, long long ndata, long long* i1,
+                                          long long* i2) {
+  *i1 = (long long)ev[2 * e] - 1;
+  *i2 = (long long)ev[2 * e + 1] - 1;
+  return !(*i1 <= 0 || *i2 <= 0 || *i1 >= ndata || *i2 >= ndata);
+}
+
+__global__ void vlor_count_kernel(const int32_t* __restrict__ ev, long long nev, long long ndata, float* cnt) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nev) return;
+  long long i1, i2;
+  if (!vlor_bins(ev, e, ndata, &i1, &i2)) return;
+  atomicAdd(cnt + i1, 1.0f);
+  atomicAdd(cnt + i2, 1.0f);
+}
+
+cudaError_t launch_vlor_count(const DevGeom& g, const int32_t* ev, long long nev, float* cnt, cudaStream_t st) {
+  if (nev <= 0) return cudaSuccess;
+  const long long ndata = (long long)g.P * g.nang * g.nrad;
+  vlor_count_kernel<<<(unsigned)((nev + 255) / 256), 256, 0, st>>>(ev, nev, ndata, cnt);
+  return cudaGetLastError();
+}
+
+// BLANKT[i] = datos_t[i]/float(RES*cnt) where cnt > 0.01 (datos_t = RES*file).
+__global__ void blankt_kernel(const float* __restrict__ cnt, const float* __restrict__ t, float res, float* bl,
+                              size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float val = cnt[i];
+  bl[i] = ((double)val > 0.01) ? __fdiv_rn(__fmul_rn(res, t[i]), __fmul_rn(res, val)) : 0.f;
+}
+
+cudaError_t launch_blankt(const DevGeom& g, const float* cnt, const float* tsino_raw, float* blankt,
+                          cudaStream_t st) {
+  const size_t n = (size_t)g.P * g.nang * g.nrad;
+  blankt_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(cnt, tsino_raw, (float)g.res, blankt, n);
+  return cudaGetLastError();
+}
+
+__global__ void vlor_split_kernel(const int32_t* __restrict__ ev, long long nev, long long ndata,
+                                  const float* __restrict__ proj, const float* __restrict__ bl, float* out) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nev) return;
+  long long i1, i2;
+  if (!vlor_bins(ev, e, ndata, &i1, &i2)) return;
+  const float valor = __fadd_rn(bl[i1], bl[i2]);
+  const float s1 = proj[i1], s2 = proj[i2];
+  const float s = __fadd_rn(s1, s2);
+  const float s_inv = (s > 0.01f) ? (float)__drcp_rn((double)s) : 0.f;
+  atomicAdd(out + i1, __fmul_rn(__fmul_rn(s1, s_inv), valor));
+  atomicAdd(out + i2, __fmul_rn(__fmul_rn(s2, s_inv), valor));
+}
+
+cudaError_t launch_vlor_split(const DevGeom& g, const int32_t* ev, long long nev, const float* proj,
+                              const float* blankt, float* out, cudaStream_t st) {
+  if (nev <= 0) return cudaSuccess;
+  const long long ndata = (long long)g.P * g.nang * g.nrad;
+  vlor_split_kernel<<<(unsigned)((nev + 255) / 256), 256, 0, st>>>(ev, nev, ndata, proj, blankt, out);
+  return cudaGetLastError();
+}
+
+}  // namespace gf

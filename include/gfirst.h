@@ -1,0 +1,185 @@
+/*
+ * gfirst.h -- C-ABI of the GB300 (sm_103a) GFIRST OSEM hot path.
+ *
+ * The reference (jlherraiz/GFIRST) is one program with no library API: its
+ * hot path is reached through the command line (GFIRST.cu:577-621), its raw
+ * file formats (GFIRST_CPU_Kernels.cpp:25-142), and, inside the program, the
+ * per-view host wrappers FORWPROJ/BACKWPROJ/... of GFIRST_GPU_Kernels.cu that
+ * osem3d() (GFIRST.cu:44-575) calls.  Each entry point below names the
+ * reference interface it replaces.  Conventions:
+ *  - plain pointers and sizes only; every call returns gf_status, never exits;
+ *  - `d_` pointers are device memory, `h_` pointers host memory;
+ *  - device arrays use the reference's layouts: images [NZS][RES][RES]
+ *    (x fastest), sinograms [P][NANG][NRAD] (radial fastest), P = planes;
+ *  - work is queued on the context's stream (gf_set_stream); calls that take
+ *    host buffers return after their results are in host memory;
+ *  - a context is used by one host thread at a time.
+ */
+#ifndef GFIRST_H
+#define GFIRST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GF_ABI_VERSION 1
+
+typedef enum gf_status {
+  GF_OK = 0,
+  GF_ERR_ARG = 1,      /* null pointer, size or mode out of range */
+  GF_ERR_GEOMETRY = 2, /* a segment has no planes, or sizes out of range */
+  GF_ERR_CUDA = 3,     /* a CUDA call failed (text in gf_last_error) */
+  GF_ERR_NOMEM = 4,    /* device allocation failed or over the memory budget */
+  GF_ERR_IO = 5,       /* file missing, unreadable or unwritable */
+  GF_ERR_STATE = 6,    /* call out of order */
+  GF_ERR_NODEV = 7,    /* no usable CUDA device */
+  GF_ERR_TIMEOUT = 8   /* a bounded device wait gave up */
+} gf_status;
+
+/* Scanner and image geometry: the compile-time constants of GFIRST.h:4-36
+ * (RES, NZS, NRAD, NANG, SPAN, NSEGMENTS, pitch, DIAM_DET, FOV), here chosen
+ * at run time.  NPT = RES and one TOF bin, as in the reference. */
+typedef struct gf_geometry {
+  int32_t res, nzs, nrad, nang, span, nseg;
+  float pitch_mm, diam_det_mm, fov_mm;
+} gf_geometry;
+
+typedef struct gf_ctx gf_ctx;
+typedef struct gf_recon gf_recon;
+
+/* ---- version, errors ---------------------------------------------------- */
+int32_t gf_abi_version(void);
+/* Text of the last error on this host thread (empty when none). */
+const char* gf_last_error(void);
+
+/* ---- geometry (GFIRST.h:4-36; GFIRST.cu:133-140, 163-176) ---------------- */
+/* The constants compiled into the reference (GFIRST.h:4-36). */
+gf_status gf_geometry_reference(gf_geometry* out);
+/* planes P = nz_acum[NSEG] (GFIRST.h:9 NSINOGS), NDATA = P*NANG*NRAD
+ * (GFIRST.h:11), NVOX = RES*RES*NZS (GFIRST.h:16). */
+gf_status gf_geometry_sizes(const gf_geometry* g, int64_t* planes, int64_t* ndata, int64_t* nvox);
+/* Segment order 0,-1,+1,-2,+2,... (GFIRST.cu:163-168), zmin
+ * (GFIRST_GPU_Kernels.cu:54) and nz_acum (GFIRST.cu:133-140, nseg+1 entries). */
+gf_status gf_segment_table(const gf_geometry* g, int32_t* idz, int32_t* zmin, int32_t* nz_acum);
+/* Sinogram bin of a line of response, GFIRST.cu:175-176. */
+gf_status gf_lor_index(const gf_geometry* g, int32_t seg_ind, int32_t iz0, int32_t itheta, int32_t ird,
+                       int64_t* lor);
+
+/* ---- context -------------------------------------------------------------- */
+/* Replaces the global set-up of osem3d() (textures and cudaMallocs,
+ * GFIRST.cu:57-83; crearTexturas, GFIRST_GPU_Kernels.cu:254-281).  Angles
+ * t with t % nsubsets == s form subset s; nsubsets = 1 is the reference's
+ * loop over all angles (NSUBSETS = 1, GFIRST.h:22). */
+gf_status gf_create(const gf_geometry* g, int32_t nsubsets, int32_t device, gf_ctx** out);
+void gf_destroy(gf_ctx* ctx);
+/* Queue later work on this cudaStream_t (NULL: the context's own stream). */
+gf_status gf_set_stream(gf_ctx* ctx, void* cuda_stream);
+gf_status gf_synchronize(gf_ctx* ctx);
+
+/* Device memory helpers for callers without a CUDA runtime of their own. */
+gf_status gf_device_alloc(gf_ctx* ctx, size_t bytes, void** d_ptr);
+gf_status gf_device_free(gf_ctx* ctx, void* d_ptr);
+/* Synchronous copies on the context's stream. */
+gf_status gf_copy_to_device(gf_ctx* ctx, void* d_dst, const void* h_src, size_t bytes);
+gf_status gf_copy_to_host(gf_ctx* ctx, void* h_dst, const void* d_src, size_t bytes);
+
+/* ---- operators on device buffers (file layouts) -------------------------- */
+/* Forward projection of every (segment, angle) view of one subset into the
+ * sinogram; bins of other subsets are left untouched.  Replaces FORWPROJ
+ * (GFIRST_GPU_Kernels.cu:105-107, kernel :40-102) looped with its scatter
+ * (GFIRST.cu:346-365).  No PSF is applied. */
+gf_status gf_forward_project(gf_ctx* ctx, const float* d_image, int32_t subset, float* d_proj);
+/* Data/projection ratio with the gap sentinel over one subset's bins:
+ * corr = data/(proj+max(bg,0)) when proj+bg >= 0.01, else -1000.
+ * Replaces the host loop of GFIRST.cu:413-430. */
+gf_status gf_ratio(gf_ctx* ctx, const float* d_proj, const float* d_data, const float* d_bg, int32_t subset,
+                   float* d_corr);
+/* Normalization mask calib = 1 where proj_blank > 0.01 and blank > 0.01, else
+ * -1000 (GFIRST.cu:453-458). */
+gf_status gf_norm_mask(gf_ctx* ctx, const float* d_proj_blank, const float* d_blank, float* d_calib);
+/* Back projection of one subset: clears numer/denom, then accumulates every
+ * (segment, angle) view of the subset in the reference's order.  Replaces
+ * BACKWPROJ (GFIRST_GPU_Kernels.cu:166-171, kernel :109-164) looped with its
+ * gather (GFIRST.cu:436-469). */
+gf_status gf_back_project(gf_ctx* ctx, const float* d_corr, const float* d_calib, int32_t subset,
+                          float* d_numer, float* d_denom);
+/* XY Gaussian PSF (9 taps, border columns passed through).  Replaces
+ * calcGaussianCoefficients + convolutionXY (GFIRST_GPU_Kernels.cu:322-364). */
+gf_status gf_psf_xy(gf_ctx* ctx, const float* d_in, float psf, float* d_out);
+/* Multiplicative update, in place: ratio numer/denom (1 where denom<0.001),
+ * XY PSF, axial filter, multiply, edge slices copied inwards.  Replaces
+ * GFIRST.cu:482-502 (dividirVxVGPU, convolutionXY, gaussian_filterZ of
+ * GFIRST_CPU_Kernels.cpp:165-187). */
+gf_status gf_image_update(gf_ctx* ctx, float* d_image, const float* d_numer, const float* d_denom, float psf_bw);
+/* Joint bilateral filter of `in` guided by `ref`.  Replaces
+ * jointbilateralfilter3D (GFIRST_GPU_Kernels.cu:508-543). */
+gf_status gf_bilateral(gf_ctx* ctx, const float* d_in, const float* d_ref, float max_ref, int32_t r,
+                       float sigma3d, float sigmai, float* d_out);
+/* VLOR end counts (d_count must be zeroed by the caller), GFIRST.cu:229-240.
+ * Events are int32 pairs of 1-based bins. */
+gf_status gf_vlor_count(gf_ctx* ctx, const int32_t* d_events, int64_t nevents, float* d_count);
+/* VLOR split of each event between its two bins in proportion to d_proj
+ * (d_out must be zeroed by the caller), GFIRST.cu:373-389. */
+gf_status gf_vlor_split(gf_ctx* ctx, const int32_t* d_events, int64_t nevents, const float* d_proj,
+                        const float* d_blankt, float* d_out);
+
+/* ---- whole reconstruction -------------------------------------------------- */
+/* The four CLI modes of GFIRST.cu:588-617: 0 projection of an image,
+ * 1 doubles sinogram + normalization, 2 doubles + triples sinograms,
+ * 3 doubles sinogram + triples VLOR list. */
+typedef struct gf_recon_params {
+  int32_t mode;
+  int32_t niter;   /* NITER, GFIRST.h:21 */
+  float psf_fw;    /* PSF_FW, GFIRST.h:26 */
+  float psf_bw;    /* PSF_BW, GFIRST.h:27 */
+  float scale_d;   /* scale_D, GFIRST.h:29 */
+  float scale_t;   /* scale_T, GFIRST.h:30 */
+} gf_recon_params;
+
+/* Reference defaults (GFIRST.h:21-30). */
+gf_status gf_recon_defaults(int32_t mode, gf_recon_params* out);
+/* Allocates every device buffer of one reconstruction and keeps it resident. */
+gf_status gf_recon_create(gf_ctx* ctx, const gf_recon_params* p, gf_recon** out);
+void gf_recon_destroy(gf_recon* r);
+/* Inputs are the parsed files (gf_read_* below): h_dsino/h_tsino 2*NDATA
+ * floats (prompts then background, before the RES scaling), h_norm NDATA
+ * floats, h_events nevents int32 pairs; unused inputs may be NULL.  Runs the
+ * normalization projection (GFIRST.cu:151-184) and the data set-up
+ * (GFIRST.cu:207-288).  Mode 0 takes h_image (NVOX floats) instead. */
+gf_status gf_recon_load(gf_recon* r, const float* h_image, const float* h_dsino, const float* h_tsino,
+                        const float* h_norm, const int32_t* h_events, int64_t nevents);
+/* Queue n full iterations (every type, every subset), GFIRST.cu:303-564. */
+gf_status gf_recon_iterate(gf_recon* r, int32_t n);
+/* Queue one sub-iteration (one type, one subset) and advance the cursor. */
+gf_status gf_recon_subiteration(gf_recon* r);
+/* Completed iterations and sub-iterations so far. */
+gf_status gf_recon_progress(const gf_recon* r, int32_t* iterations, int64_t* subiterations);
+/* Image of type 0 (doubles) or 1 (triples), file layout, NVOX floats.
+ * scaled != 0 applies the output scaling and mask of GFIRST.cu:532-549. */
+gf_status gf_recon_get_image(gf_recon* r, int32_t type, int32_t scaled, float* h_out);
+/* proj_ref.raw contents (GFIRST.cu:183-184), NDATA floats. */
+gf_status gf_recon_get_proj_ref(gf_recon* r, float* h_out);
+/* SINOG_VLOR.raw contents of the last triples sub-iteration (GFIRST.cu:391-394). */
+gf_status gf_recon_get_sinog_vlor(gf_recon* r, float* h_out);
+
+/* ---- raw files (GFIRST_CPU_Kernels.cpp:25-142, GFIRST.cu:229-240) --------- */
+/* ReadSinogram_Type (GFIRST_CPU_Kernels.cpp:104-142): int32 file, re-read as
+ * float32 when the largest int exceeds 1e6; h_out gets 2*ndata floats (zeros
+ * past the end of the file; a missing file gives GF_ERR_IO and zeros). */
+gf_status gf_read_sinogram(const char* path, int64_t ndata, float* h_out);
+/* ReadImage (GFIRST_CPU_Kernels.cpp:58-66): nvox floats. */
+gf_status gf_read_image(const char* path, int64_t nvox, float* h_out);
+/* VLOR list as GFIRST.cu:232-240 consumes it, including the extra pass of its
+ * while(!feof) loop over the last record.  With h_events NULL only the count
+ * is returned; otherwise up to *nevents pairs are written. */
+gf_status gf_read_vlor(const char* path, int32_t* h_events, int64_t* nevents);
+/* WriteImage (GFIRST_CPU_Kernels.cpp:25-33). */
+gf_status gf_write_raw(const char* path, const float* h_data, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GFIRST_H */

@@ -1,0 +1,314 @@
+"""GPU parity: the sm_103a library, called through its C-ABI, against the CPU
+oracle and against the golden outputs of the reference program.
+
+Tolerances (relative L2 unless stated): indices and the integer VLOR counts
+bit-exact; back projection, ratio, normalization mask, XY PSF and the image
+update bit-exact (same operation order and rounding as the oracle); forward
+projection 1e-4 (it sums the same samples with a factored interpolation);
+images after the stated iterations 1e-3.
+"""
+import subprocess
+
+import numpy as np
+import pytest
+
+import gfo
+import gfo_io
+import inputs
+
+pytestmark = pytest.mark.gpu
+
+FP_TOL = 1e-4
+IMG_TOL = 1e-3
+
+
+@pytest.fixture(scope="module")
+def gf():
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import gfirst_gb300
+
+    if not gfirst_gb300.gpu_available():
+        pytest.fail("no sm_103 GPU available to the library")
+    return gfirst_gb300
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def case(name):
+    return inputs.GEOMS[name]
+
+
+def image(o, seed, lo=0.0, hi=3.0):
+    return np.random.RandomState(seed).uniform(lo, hi, o.nvox).astype(np.float32)
+
+
+# ---------------------------------------------------------------- projector
+@pytest.mark.parametrize("name,nsub,subset", [("tiny", 1, 0), ("tiny", 3, 2), ("tinyb", 4, 1), ("small", 1, 0),
+                                              ("small", 8, 5)])
+def test_forward_projection_matches_oracle(gf, name, nsub, subset):
+    geo = case(name)
+    o = gfo.Oracle(geo)
+    ctx = gf.Context(gf.Geometry(*geo), nsub=nsub)
+    img = inputs.phantom(name, 5).ravel() if name != "tiny" else image(o, 5, -1.0, 3.0)
+    proj = ctx.array(o.ndata).upload(np.full(o.ndata, -7.0, np.float32))
+    ctx.forward_project(ctx.put(img), subset, proj)
+    got = proj.download()
+    want = o.fp(img, nsub, subset, out=np.full(o.ndata, -7.0, np.float32))
+    theta = (np.arange(o.ndata) // geo[2]) % geo[3]
+    insub = theta % nsub == subset
+    assert np.array_equal(got[~insub], want[~insub])  # other subsets untouched
+    assert rel(got[insub], want[insub]) < FP_TOL
+    assert np.abs(got - want).max() <= 1e-4 * np.abs(want).max()
+
+
+def test_forward_projection_of_constant_is_exact(gf):
+    geo = case("small")
+    o = gfo.Oracle(geo)
+    ctx = gf.Context(gf.Geometry(*geo))
+    proj = ctx.array(o.ndata)
+    ctx.forward_project(ctx.put(np.ones(o.nvox, np.float32)), 0, proj)
+    assert np.array_equal(proj.download(), np.full(o.ndata, geo[0] + 1, np.float32))
+
+
+def test_ratio_and_mask_bit_exact(gf):
+    geo = case("tinyb")
+    o = gfo.Oracle(geo)
+    rs = np.random.RandomState(9)
+    proj = rs.uniform(-0.02, 5.0, o.ndata).astype(np.float32)
+    data = rs.poisson(3.0, o.ndata).astype(np.float32)
+    bg = rs.uniform(-0.5, 0.5, o.ndata).astype(np.float32)
+    ctx = gf.Context(gf.Geometry(*geo), nsub=3)
+    corr = ctx.array(o.ndata).upload(np.zeros(o.ndata, np.float32))
+    ctx.ratio(ctx.put(proj), ctx.put(data), ctx.put(bg), 1, corr)
+    want = o.ratio(proj, data, bg, 3, 1)
+    assert np.array_equal(corr.download(), want)
+    pb, bl = rs.uniform(0, 0.02, o.ndata).astype(np.float32), rs.uniform(0, 0.02, o.ndata).astype(np.float32)
+    cal = ctx.array(o.ndata)
+    ctx.norm_mask(ctx.put(pb), ctx.put(bl), cal)
+    assert np.array_equal(cal.download(), o.calib(pb, bl))
+
+
+def corr_calib(o, seed):
+    rs = np.random.RandomState(seed)
+    corr = rs.uniform(0.0, 3.0, o.ndata).astype(np.float32)
+    corr[rs.uniform(size=o.ndata) < 0.03] = -1000.0
+    calib = np.where(rs.uniform(size=o.ndata) < 0.05, -1000.0, 1.0).astype(np.float32)
+    return corr, calib
+
+
+# ---------------------------------------------------------------- back projector
+@pytest.mark.parametrize("name,nsub,subset", [("tiny", 1, 0), ("tinyb", 3, 2), ("small", 1, 0), ("small", 4, 3)])
+def test_back_projection_bit_exact(gf, name, nsub, subset):
+    geo = case(name)
+    o = gfo.Oracle(geo)
+    corr, calib = corr_calib(o, 17)
+    ctx = gf.Context(gf.Geometry(*geo), nsub=nsub)
+    numer, denom = ctx.array(o.nvox), ctx.array(o.nvox)
+    ctx.back_project(ctx.put(corr), ctx.put(calib), subset, numer, denom)
+    wn, wd = o.bp(corr, calib, nsub, subset)
+    assert np.array_equal(numer.download(), wn)
+    assert np.array_equal(denom.download(), wd)
+
+
+# ---------------------------------------------------------------- update chain
+@pytest.mark.parametrize("name", ["tiny", "small"])
+def test_psf_and_update_bit_exact(gf, name):
+    geo = case(name)
+    o = gfo.Oracle(geo)
+    ctx = gf.Context(gf.Geometry(*geo))
+    img = image(o, 21)
+    out = ctx.array(o.nvox)
+    ctx.psf_xy(ctx.put(img), 1.5, out)
+    assert np.array_equal(out.download(), o.conv_xy(img, 1.5))
+    rs = np.random.RandomState(22)
+    numer = rs.uniform(0, 4, o.nvox).astype(np.float32)
+    denom = rs.uniform(0, 4, o.nvox).astype(np.float32)
+    denom[rs.uniform(size=o.nvox) < 0.05] = 0.0005
+    dimg = ctx.put(img)
+    ctx.image_update(dimg, ctx.put(numer), ctx.put(denom), 1.5)
+    assert np.array_equal(dimg.download(), o.update(img, numer, denom, 1.5))
+
+
+def test_bilateral_matches_oracle(gf):
+    geo = case("tinyb")
+    o = gfo.Oracle(geo)
+    ctx = gf.Context(gf.Geometry(*geo))
+    inp, ref = image(o, 31), image(o, 32)
+    mx = float(ref.max())
+    out = ctx.array(o.nvox)
+    ctx.bilateral(ctx.put(inp), ctx.put(ref), mx, out)
+    got, want = out.download(), o.bilateral(inp, ref, mx)
+    assert np.array_equal(got == 0, want == 0)  # the unsigned-window zeros
+    assert rel(got, want) < 1e-5
+
+
+# ---------------------------------------------------------------- VLOR
+def test_vlor_count_exact_and_split(gf):
+    geo = case("tiny")
+    o = gfo.Oracle(geo)
+    ev = gfo_io.read_vlor(inputs.case_files("tiny")["vlor.raw"])
+    ctx = gf.Context(gf.Geometry(*geo))
+    dev = ctx.put(ev, np.int32)
+    cnt = ctx.array(o.ndata).zero()
+    ctx.vlor_count(dev, len(ev), cnt)
+    assert np.array_equal(cnt.download(), o.vlor_count(ev))
+    rs = np.random.RandomState(4)
+    proj = rs.uniform(0, 2, o.ndata).astype(np.float32)
+    bl = rs.uniform(0, 1, o.ndata).astype(np.float32)
+    out = ctx.array(o.ndata).zero()
+    ctx.vlor_split(dev, len(ev), ctx.put(proj), ctx.put(bl), out)
+    assert rel(out.download(), o.vlor_split(ev, proj, bl)) < 1e-6
+
+
+# ---------------------------------------------------------------- reconstruction
+def parsed(name):
+    files = inputs.case_files(name)
+    ndata, nvox = inputs.sizes(name)
+    return dict(image=gfo_io.read_image(files["img.raw"], nvox),
+                dsino=gfo_io.read_sinogram_type(files["sinoD.raw"], ndata),
+                tsino=gfo_io.read_sinogram_type(files["sinoT.raw"], ndata),
+                norm=gfo_io.read_sinogram_type(files["norm.raw"], ndata)[:ndata],
+                events=gfo_io.read_vlor(files["vlor.raw"]))
+
+
+@pytest.mark.parametrize("name", ["tiny", "tinyb"])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3])
+def test_recon_matches_reference_golden(gf, name, mode):
+    geo = case(name)
+    z = np.load(inputs.__file__.replace("inputs.py", f"golden_{name}.npz"))
+    d = parsed(name)
+    ctx = gf.Context(gf.Geometry(*geo))
+    r = gf.Recon(ctx, mode, niter=20)
+    if mode == 0:
+        r.load(image=d["image"])
+        assert rel(r.proj_ref(), z["m0_proj_ref"]) < FP_TOL
+        return
+    r.load(dsino=d["dsino"], tsino=d["tsino"] if mode >= 2 else None, norm=d["norm"],
+           events=d["events"] if mode == 3 else None)
+    assert rel(r.proj_ref(), z[f"m{mode}_proj_ref"]) < FP_TOL
+    r.iterate(20)
+    assert rel(r.image(0, scaled=True), z[f"m{mode}_img_D"]) < IMG_TOL
+    if mode >= 2:
+        assert rel(r.image(1, scaled=True), z[f"m{mode}_img_T"]) < IMG_TOL
+    if mode == 3:
+        assert rel(r.sinog_vlor(), z["m3_sinog_vlor"]) < IMG_TOL
+
+
+@pytest.mark.parametrize("mode,nsub", [(1, 4), (2, 2), (3, 4)])
+def test_recon_with_subsets_matches_oracle(gf, mode, nsub):
+    geo = case("tinyb")
+    d = parsed("tinyb")
+    o = gfo.Oracle(geo)
+    o64 = gfo.Oracle(geo, "f64")
+    kw = dict(dsino=d["dsino"], tsino=d["tsino"], norm=d["norm"], ev=d["events"])
+    want = o.recon(mode, nsub=nsub, niter=3, **kw)
+    exact = o64.recon(mode, nsub=nsub, niter=3, **kw)
+    ctx = gf.Context(gf.Geometry(*geo), nsub=nsub)
+    r = gf.Recon(ctx, mode, niter=3)
+    r.load(dsino=d["dsino"], tsino=d["tsino"], norm=d["norm"], events=d["events"])
+    r.iterate(3)
+    for t, key in ((0, "img_d"), (1, "img_t")):
+        if mode == 1 and t == 1:
+            continue
+        got = r.image(t)
+        assert rel(got, want[key]) < IMG_TOL
+        assert rel(got, exact[key]) < IMG_TOL  # error against the FP64 oracle
+
+
+def test_recon_small_geometry_mode1_subsets(gf):
+    geo = case("small")
+    d = parsed("small")
+    o = gfo.Oracle(geo)
+    want = o.recon(1, nsub=4, niter=2, dsino=d["dsino"], norm=d["norm"])
+    ctx = gf.Context(gf.Geometry(*geo), nsub=4)
+    r = gf.Recon(ctx, 1, niter=2)
+    r.load(dsino=d["dsino"], norm=d["norm"])
+    r.iterate(2)
+    assert rel(r.image(0), want["img_d"]) < IMG_TOL
+
+
+def test_recon_is_deterministic(gf):
+    geo = case("tinyb")
+    d = parsed("tinyb")
+    outs = []
+    for _ in range(2):
+        ctx = gf.Context(gf.Geometry(*geo), nsub=2)
+        r = gf.Recon(ctx, 2, niter=2)
+        r.load(dsino=d["dsino"], tsino=d["tsino"], norm=d["norm"])
+        r.iterate(2)
+        outs.append((r.image(0), r.image(1)))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_cli_end_to_end_matches_reference(gf, tmp_path):
+    name = "tiny"
+    geo = case(name)
+    z = np.load(inputs.__file__.replace("inputs.py", f"golden_{name}.npz"))
+    for k, v in inputs.case_files(name).items():
+        (tmp_path / k).write_bytes(v)
+    gs = ",".join(str(x) for x in geo)
+    cmd = [str(gf.CLI_PATH), "--geometry", gs, "--iterations", "20", "sinoD.raw", "sinoT.raw", "norm.raw",
+           "vlor.raw"]
+    out = subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    ld = lambda f: np.fromfile(tmp_path / f, np.float32)  # noqa: E731
+    assert rel(ld("proj_ref.raw"), z["m3_proj_ref"]) < FP_TOL
+    assert rel(ld("img_GPU_D_ITER20.raw"), z["m3_img_D"]) < IMG_TOL
+    assert rel(ld("img_GPU_T_ITER20.raw"), z["m3_img_T"]) < IMG_TOL
+    assert rel(ld("SINOG_VLOR.raw"), z["m3_sinog_vlor"]) < IMG_TOL
+
+
+# ---------------------------------------------------------------- full preclinical size
+@pytest.fixture(scope="module")
+def c2(gf):
+    g = gf.Geometry.preclinical()
+    return g, gf.Context(g, nsub=16)
+
+
+def test_preclinical_forward_projection_subset_matches_oracle(gf, c2):
+    g, ctx = c2
+    o = gfo.Oracle(g.tuple())
+    img = np.random.RandomState(2).uniform(0, 1, o.nvox).astype(np.float32)
+    proj = ctx.array(o.ndata).zero()
+    ctx.forward_project(ctx.put(img), 5, proj)
+    want = o.fp(img, 16, 5)
+    got = proj.download()
+    assert rel(got, want) < FP_TOL
+
+
+def test_preclinical_back_projection_subset_bit_exact(gf, c2):
+    g, ctx = c2
+    o = gfo.Oracle(g.tuple())
+    corr, calib = corr_calib(o, 8)
+    numer, denom = ctx.array(o.nvox), ctx.array(o.nvox)
+    ctx.back_project(ctx.put(corr), ctx.put(calib), 3, numer, denom)
+    wn, wd = o.bp(corr, calib, 16, 3)
+    assert np.array_equal(numer.download(), wn) and np.array_equal(denom.download(), wd)
+
+
+def test_preclinical_properties(gf, c2):
+    """Size-independent checks on the full 128x128x159 / 4319-plane geometry."""
+    g, ctx = c2
+    P, ndata, nvox = gf.sizes(g)
+    ones = ctx.put(np.ones(nvox, np.float32))
+    proj = ctx.array(ndata).zero()
+    for s in range(16):
+        ctx.forward_project(ones, s, proj)
+    assert np.array_equal(proj.download(), np.full(ndata, g.res + 1, np.float32))  # every ray: RES+1 samples
+    rs = np.random.RandomState(1)
+    a, b = rs.uniform(0, 1, nvox).astype(np.float32), rs.uniform(0, 1, nvox).astype(np.float32)
+    pa, pb, pab = ctx.array(ndata).zero(), ctx.array(ndata).zero(), ctx.array(ndata).zero()
+    ctx.forward_project(ctx.put(a), 7, pa)
+    ctx.forward_project(ctx.put(b), 7, pb)
+    ctx.forward_project(ctx.put(2.0 * a + b), 7, pab)
+    assert rel(pab.download(), 2.0 * pa.download() + pb.download()) < 1e-5  # linearity
+    ones_s = ctx.put(np.ones(ndata, np.float32))
+    numer, denom = ctx.array(nvox), ctx.array(nvox)
+    ctx.back_project(ones_s, ones_s, 9, numer, denom)
+    n, d = numer.download(), denom.download()
+    assert np.array_equal(n, d) and n.max() > 0  # identical channels give identical sums
