@@ -18,6 +18,7 @@ _HERE = Path(__file__).resolve().parent
 LIB_PATH = _HERE / "lib" / "libgfirst.so"
 CLI_PATH = _HERE / "lib" / "gfirst"
 
+STAGES = {"psf": 0, "fp": 1, "vlor": 2, "bp": 3, "update": 4, "bilateral": 5}
 STATUS = {0: "GF_OK", 1: "GF_ERR_ARG", 2: "GF_ERR_GEOMETRY", 3: "GF_ERR_CUDA", 4: "GF_ERR_NOMEM",
           5: "GF_ERR_IO", 6: "GF_ERR_STATE", 7: "GF_ERR_NODEV", 8: "GF_ERR_TIMEOUT"}
 
@@ -196,6 +197,11 @@ class Context:
     def sync(self) -> None:
         _ck(lib().gf_synchronize(self.h))
 
+    def launches(self) -> int:
+        n = ctypes.c_int64()
+        _ck(lib().gf_kernel_launches(self.h, ctypes.byref(n)))
+        return n.value
+
     # operators on device arrays (reference file layouts)
     def forward_project(self, img: DeviceArray, subset: int, proj: DeviceArray) -> None:
         _ck(lib().gf_forward_project(self.h, img.p, subset, proj.p))
@@ -279,6 +285,14 @@ class Recon:
         out = np.empty(self.ctx.ndata, np.float32)
         _ck(lib().gf_recon_get_proj_ref(self.h, _ptr(out)))
         return out
+
+    def profile(self, enable: bool = True) -> None:
+        _ck(lib().gf_recon_profile(self.h, int(enable)))
+
+    def profile_read(self, stage: int) -> tuple:
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        _ck(lib().gf_recon_profile_read(self.h, stage, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
 
     def sinog_vlor(self) -> np.ndarray:
         out = np.empty(self.ctx.ndata, np.float32)

@@ -118,6 +118,12 @@ FpArgs gf_ctx::fp_args(int subset, const float* img_zfast) const {
 
 extern "C" {
 
+gf_status gf_kernel_launches(const gf_ctx* c, int64_t* n) {
+  if (!c || !n) return set_error(GF_ERR_ARG, "null argument");
+  *n = c->launches;
+  return GF_OK;
+}
+
 int32_t gf_abi_version(void) { return GF_ABI_VERSION; }
 
 const char* gf_last_error(void) { return g_err.c_str(); }
@@ -296,6 +302,21 @@ gf_status gf_device_free(gf_ctx* c, void* d) {
   return GF_OK;
 }
 
+gf_status gf_host_alloc(size_t bytes, void** h) {
+  if (!h) return set_error(GF_ERR_ARG, "null argument");
+  cudaError_t e = cudaMallocHost(h, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_error(e, "cudaMallocHost");
+  }
+  return GF_OK;
+}
+
+gf_status gf_host_free(void* h) {
+  GF_CK(cudaFreeHost(h));
+  return GF_OK;
+}
+
 gf_status gf_copy_to_device(gf_ctx* c, void* d, const void* h, size_t bytes) {
   if (!c || (!d && bytes) || (!h && bytes)) return set_error(GF_ERR_ARG, "null argument");
   GF_CK(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, c->stream));
@@ -321,10 +342,10 @@ gf_status gf_forward_project(gf_ctx* c, const float* d_image, int32_t subset, fl
   GF_TRY(check_subset(c, subset));
   if (!d_image || !d_proj) return set_error(GF_ERR_ARG, "null buffer");
   GF_TRY(c->ensure_scratch());
-  GF_CK(launch_file_to_zfast(c->dg, d_image, c->s_img, c->stream));
+  GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_image, c->s_img, c->stream));
   FpArgs a = c->fp_args(subset, c->s_img);
   a.proj_full = d_proj;
-  GF_CK(launch_fp(a, c->fps, c->stream));
+  GF_LAUNCH(c, launch_fp(a, c->fps, c->stream));
   return GF_OK;
 }
 
@@ -332,13 +353,13 @@ gf_status gf_ratio(gf_ctx* c, const float* d_proj, const float* d_data, const fl
                    float* d_corr) {
   GF_TRY(check_subset(c, subset));
   if (!d_proj || !d_data || !d_bg || !d_corr) return set_error(GF_ERR_ARG, "null buffer");
-  GF_CK(launch_ratio_file(c->dg, subset, d_proj, d_data, d_bg, d_corr, c->stream));
+  GF_LAUNCH(c, launch_ratio_file(c->dg, subset, d_proj, d_data, d_bg, d_corr, c->stream));
   return GF_OK;
 }
 
 gf_status gf_norm_mask(gf_ctx* c, const float* d_pb, const float* d_b, float* d_calib) {
   if (!c || !d_pb || !d_b || !d_calib) return set_error(GF_ERR_ARG, "null argument");
-  GF_CK(launch_norm_mask(c->dg, d_pb, d_b, d_calib, c->stream));
+  GF_LAUNCH(c, launch_norm_mask(c->dg, d_pb, d_b, d_calib, c->stream));
   return GF_OK;
 }
 
@@ -348,32 +369,32 @@ gf_status gf_back_project(gf_ctx* c, const float* d_corr, const float* d_calib, 
   if (!d_corr || !d_calib || !d_numer || !d_denom) return set_error(GF_ERR_ARG, "null buffer");
   GF_TRY(c->ensure_scratch());
   const int na = c->plan.sub_nang[subset];
-  GF_CK(launch_corrcal_from_file(c->dg, c->d_rowmap, subset, na, d_corr, d_calib, c->s_cc, c->stream));
+  GF_LAUNCH(c, launch_corrcal_from_file(c->dg, c->d_rowmap, subset, na, d_corr, d_calib, c->s_cc, c->stream));
   BpArgs b{c->dg, subset, na, c->s_cc, c->s_numer, c->s_denom};
-  GF_CK(launch_bp(b, c->stream));
-  GF_CK(launch_zfast_to_file(c->dg, c->s_numer, 1.f, 0, d_numer, c->stream));
-  GF_CK(launch_zfast_to_file(c->dg, c->s_denom, 1.f, 0, d_denom, c->stream));
+  GF_LAUNCH(c, launch_bp(b, c->stream));
+  GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_numer, 1.f, 0, d_numer, c->stream));
+  GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_denom, 1.f, 0, d_denom, c->stream));
   return GF_OK;
 }
 
 gf_status gf_psf_xy(gf_ctx* c, const float* d_in, float psf, float* d_out) {
   if (!c || !d_in || !d_out) return set_error(GF_ERR_ARG, "null argument");
   GF_TRY(c->ensure_scratch());
-  GF_CK(launch_file_to_zfast(c->dg, d_in, c->s_img, c->stream));
-  GF_CK(launch_conv_xy(c->dg, c->s_img, nullptr, gauss9(psf), c->s_img2, c->stream));
-  GF_CK(launch_zfast_to_file(c->dg, c->s_img2, 1.f, 0, d_out, c->stream));
+  GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_in, c->s_img, c->stream));
+  GF_LAUNCH(c, launch_conv_xy(c->dg, c->s_img, nullptr, gauss9(psf), c->s_img2, c->stream));
+  GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_img2, 1.f, 0, d_out, c->stream));
   return GF_OK;
 }
 
 gf_status gf_image_update(gf_ctx* c, float* d_image, const float* d_numer, const float* d_denom, float psf_bw) {
   if (!c || !d_image || !d_numer || !d_denom) return set_error(GF_ERR_ARG, "null argument");
   GF_TRY(c->ensure_scratch());
-  GF_CK(launch_file_to_zfast(c->dg, d_numer, c->s_numer, c->stream));
-  GF_CK(launch_file_to_zfast(c->dg, d_denom, c->s_denom, c->stream));
-  GF_CK(launch_file_to_zfast(c->dg, d_image, c->s_img, c->stream));
-  GF_CK(launch_conv_xy(c->dg, c->s_numer, c->s_denom, gauss9(psf_bw), c->s_img2, c->stream));
-  GF_CK(launch_zfilter_update(c->dg, c->s_img2, c->s_img, gauss5(), c->s_numer, c->stream));
-  GF_CK(launch_zfast_to_file(c->dg, c->s_numer, 1.f, 0, d_image, c->stream));
+  GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_numer, c->s_numer, c->stream));
+  GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_denom, c->s_denom, c->stream));
+  GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_image, c->s_img, c->stream));
+  GF_LAUNCH(c, launch_conv_xy(c->dg, c->s_numer, c->s_denom, gauss9(psf_bw), c->s_img2, c->stream));
+  GF_LAUNCH(c, launch_zfilter_update(c->dg, c->s_img2, c->s_img, gauss5(), c->s_numer, c->stream));
+  GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_numer, 1.f, 0, d_image, c->stream));
   return GF_OK;
 }
 
@@ -383,23 +404,23 @@ gf_status gf_bilateral(gf_ctx* c, const float* d_in, const float* d_ref, float m
   if (r < 0 || r > 4) return set_error(GF_ERR_ARG, "window radius must be in [0, 4]");
   GF_TRY(c->ensure_scratch());
   GF_TRY(c->ensure_gtab(sigma3d));
-  GF_CK(launch_file_to_zfast(c->dg, d_in, c->s_img, c->stream));
-  GF_CK(launch_file_to_zfast(c->dg, d_ref, c->s_img2, c->stream));
-  GF_CK(launch_bilateral(c->dg, c->s_img, c->s_img2, nullptr, max_ref, r, sigmai, c->d_gtab, c->s_numer, c->stream));
-  GF_CK(launch_zfast_to_file(c->dg, c->s_numer, 1.f, 0, d_out, c->stream));
+  GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_in, c->s_img, c->stream));
+  GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_ref, c->s_img2, c->stream));
+  GF_LAUNCH(c, launch_bilateral(c->dg, c->s_img, c->s_img2, nullptr, max_ref, r, sigmai, c->d_gtab, c->s_numer, c->stream));
+  GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_numer, 1.f, 0, d_out, c->stream));
   return GF_OK;
 }
 
 gf_status gf_vlor_count(gf_ctx* c, const int32_t* d_ev, int64_t n, float* d_count) {
   if (!c || (!d_ev && n) || !d_count || n < 0) return set_error(GF_ERR_ARG, "bad argument");
-  GF_CK(launch_vlor_count(c->dg, d_ev, n, d_count, c->stream));
+  GF_LAUNCH(c, launch_vlor_count(c->dg, d_ev, n, d_count, c->stream));
   return GF_OK;
 }
 
 gf_status gf_vlor_split(gf_ctx* c, const int32_t* d_ev, int64_t n, const float* d_proj, const float* d_blankt,
                         float* d_out) {
   if (!c || (!d_ev && n) || !d_proj || !d_blankt || !d_out || n < 0) return set_error(GF_ERR_ARG, "bad argument");
-  GF_CK(launch_vlor_split(c->dg, d_ev, n, d_proj, d_blankt, d_out, c->stream));
+  GF_LAUNCH(c, launch_vlor_split(c->dg, d_ev, n, d_proj, d_blankt, d_out, c->stream));
   return GF_OK;
 }
 

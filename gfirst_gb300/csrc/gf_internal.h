@@ -20,6 +20,14 @@ gf_status cuda_error(cudaError_t e, const char* what);
     if (e__ != cudaSuccess) return ::gf::cuda_error(e__, #x);   \
   } while (0)
 
+// Launch one of this library's kernels: count it and check the launch.
+#define GF_LAUNCH(ctx, x)                                       \
+  do {                                                          \
+    (ctx)->launches++;                                          \
+    cudaError_t e__ = (x);                                      \
+    if (e__ != cudaSuccess) return ::gf::cuda_error(e__, #x);   \
+  } while (0)
+
 #define GF_TRY(x)                         \
   do {                                    \
     gf_status s__ = (x);                  \
@@ -54,6 +62,7 @@ struct gf_ctx {
   float* d_gtab = nullptr;
   float gtab_sigma = -1.f;
   // scratch of the operator entry points, allocated on first use
+  int64_t launches = 0;  // kernels launched by this context
   float* s_img = nullptr;
   float* s_img2 = nullptr;
   float* s_numer = nullptr;
@@ -92,16 +101,29 @@ struct gf_recon {
   float* blankt = nullptr;
   float* datos_v = nullptr;
   float* d_max = nullptr;
+  float* stage = nullptr;  // device staging of host inputs (3*NDATA floats)
   gf::Taps9 g_fw{}, g_bw{};
   gf::Taps5 g5{};
   int iters_done = 0;
   int64_t subs_done = 0;
   int cur_type = 0, cur_sub = 0;
 
+  // stage profiling
+  struct StageEv {
+    int stage;
+    cudaEvent_t a, b;
+  };
+  bool prof = false;
+  std::vector<StageEv> evs;
+  size_t ev_used = 0;
+  void stage_begin(int stage);
+  void stage_end();
+
   gf_status alloc(size_t bytes, void** p);
   template <class T> gf_status alloc_t(size_t n, T** q) {
     return alloc(n * sizeof(T), reinterpret_cast<void**>(q));
   }
   gf_status subiteration(int type, int subset);
+  gf_status init_images();
   gf_status project_all(const float* img_zfast, float* proj_full);
 };

@@ -31,12 +31,48 @@ gf_status gf_recon::alloc(size_t bytes, void** q) {
   return GF_OK;
 }
 
+void gf_recon::stage_begin(int stage) {
+  if (!prof) return;
+  if (ev_used == evs.size()) {
+    StageEv e{stage, nullptr, nullptr};
+    cudaEventCreate(&e.a);
+    cudaEventCreate(&e.b);
+    evs.push_back(e);
+  }
+  evs[ev_used].stage = stage;
+  cudaEventRecord(evs[ev_used].a, ctx->stream);
+}
+
+void gf_recon::stage_end() {
+  if (!prof) return;
+  cudaEventRecord(evs[ev_used].b, ctx->stream);
+  ev_used++;
+}
+
 gf_status gf_recon::project_all(const float* img_zfast, float* proj_full) {
   for (int s = 0; s < ctx->plan.nsub; s++) {
     FpArgs a = ctx->fp_args(s, img_zfast);
     a.proj_full = proj_full;
-    GF_CK(launch_fp(a, ctx->fps, ctx->stream));
+    GF_LAUNCH(ctx, launch_fp(a, ctx->fps, ctx->stream));
   }
+  return GF_OK;
+}
+
+// STEP 3, initial images (GFIRST.cu:282-288), and the mode-3 triples
+// projection that weights the VLOR split (refreshed subset by subset later).
+gf_status gf_recon::init_images() {
+  gf_ctx* c = ctx;
+  cudaStream_t st = c->stream;
+  GF_LAUNCH(c, launch_cylinder(c->dg, 1.0f, img[0], st));
+  GF_LAUNCH(c, launch_cylinder(c->dg, p.mode == 1 ? 0.0f : 1.0f, img[1], st));
+  if (p.mode == 3) {
+    GF_LAUNCH(c, launch_conv_xy(c->dg, img[1], nullptr, g_fw, psf, st));
+    GF_TRY(project_all(psf, proj_t));
+    GF_CK(cudaMemsetAsync(datos_v, 0, c->plan.ndata * sizeof(float), st));
+  }
+  iters_done = 0;
+  subs_done = 0;
+  cur_type = cur_sub = 0;
   return GF_OK;
 }
 
@@ -46,32 +82,46 @@ gf_status gf_recon::subiteration(int t, int s) {
   cudaStream_t st = c->stream;
   const int na = pl.sub_nang[s];
   const int64_t off = pl.sub_off[s];
-  GF_CK(launch_conv_xy(c->dg, img[t], nullptr, g_fw, psf, st));
+  stage_begin(GF_STAGE_PSF);
+  GF_LAUNCH(c, launch_conv_xy(c->dg, img[t], nullptr, g_fw, psf, st));
+  stage_end();
   FpArgs a = c->fp_args(s, psf);
   if (p.mode == 3 && t == 1) {
     a.proj_full = proj_t;
-    GF_CK(launch_fp(a, c->fps, st));
+    stage_begin(GF_STAGE_FP);
+    GF_LAUNCH(c, launch_fp(a, c->fps, st));
+    stage_end();
+    stage_begin(GF_STAGE_VLOR);
     GF_CK(cudaMemsetAsync(datos_v, 0, (size_t)pl.ndata * sizeof(float), st));
-    GF_CK(launch_vlor_split(c->dg, events, nev, proj_t, blankt, datos_v, st));
-    GF_CK(launch_ratio_gather(c->dg, c->d_rowmap, s, na, proj_t, datos_v, dbg[1] + off, cal + off, corrcal, st));
+    GF_LAUNCH(c, launch_vlor_split(c->dg, events, nev, proj_t, blankt, datos_v, st));
+    GF_LAUNCH(c, launch_ratio_gather(c->dg, c->d_rowmap, s, na, proj_t, datos_v, dbg[1] + off, cal + off, corrcal, st));
+    stage_end();
   } else {
     a.dbg = dbg[t] + off;
     a.cal = cal + off;
     a.corrcal = corrcal;
-    GF_CK(launch_fp(a, c->fps, st));
+    stage_begin(GF_STAGE_FP);
+    GF_LAUNCH(c, launch_fp(a, c->fps, st));
+    stage_end();
   }
   BpArgs b{c->dg, s, na, corrcal, numer, denom};
-  GF_CK(launch_bp(b, st));
-  GF_CK(launch_conv_xy(c->dg, numer, denom, g_bw, ctmp, st));
-  GF_CK(launch_zfilter_update(c->dg, ctmp, img[t], g5, img_alt, st));
+  stage_begin(GF_STAGE_BP);
+  GF_LAUNCH(c, launch_bp(b, st));
+  stage_end();
+  stage_begin(GF_STAGE_UPDATE);
+  GF_LAUNCH(c, launch_conv_xy(c->dg, numer, denom, g_bw, ctmp, st));
+  GF_LAUNCH(c, launch_zfilter_update(c->dg, ctmp, img[t], g5, img_alt, st));
+  stage_end();
   float* tmp = img[t];
   img[t] = img_alt;
   img_alt = tmp;
   if (t == 1 && s == pl.nsub - 1) {
     // GFIRST.cu:512-524: r=4, sigma3D=0.75, sigmaI=0.025, max_ref over the doubles image
-    GF_CK(launch_max_nonneg(c->dg, img[0], d_max, st));
-    GF_CK(launch_bilateral(c->dg, img[1], img[0], d_max, 0.f, 4, 0.025f, c->d_gtab, filt, st));
-    GF_CK(launch_blend(c->dg, img[1], filt, st));
+    stage_begin(GF_STAGE_BILATERAL);
+    GF_LAUNCH(c, launch_max_nonneg(c->dg, img[0], d_max, st));
+    GF_LAUNCH(c, launch_bilateral(c->dg, img[1], img[0], d_max, 0.f, 4, 0.025f, c->d_gtab, filt, st));
+    GF_LAUNCH(c, launch_blend(c->dg, img[1], filt, st));
+    stage_end();
   }
   return GF_OK;
 }
@@ -144,6 +194,10 @@ gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out)
 void gf_recon_destroy(gf_recon* r) {
   if (!r) return;
   if (r->ctx) cudaStreamSynchronize(r->ctx->stream);
+  for (auto& e : r->evs) {
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
   for (auto& b : r->owned) cudaFree(b.p);
   delete r;
 }
@@ -160,14 +214,13 @@ gf_status gf_recon_load(gf_recon* r, const float* h_image, const float* h_dsino,
   if (mode >= 2 && !h_tsino) return set_error(GF_ERR_ARG, "modes 2-3 need a triples sinogram");
   if (mode == 3 && (nevents < 0 || (nevents > 0 && !h_events))) return set_error(GF_ERR_ARG, "mode 3 needs VLOR events");
   GF_CK(cudaSetDevice(c->device));
-  // staging buffer for the host inputs, freed at the end of the load
-  float* stage = nullptr;
+  // device staging of the host inputs, kept for later loads
   size_t stage_n = (size_t)2 * pl.ndata + (size_t)pl.ndata;
   if (mode == 0) stage_n = pl.nvox;
-  GF_CK(cudaMalloc(&stage, stage_n * sizeof(float)));
+  if (!r->stage) GF_TRY(r->alloc_t(stage_n, &r->stage));
+  float* stage = r->stage;
   auto done = [&](gf_status s) {
     cudaStreamSynchronize(st);
-    cudaFree(stage);
     return s;
   };
   auto ck = [&](cudaError_t e, const char* w) { return e == cudaSuccess ? GF_OK : cuda_error(e, w); };
@@ -204,20 +257,16 @@ gf_status gf_recon_load(gf_recon* r, const float* h_image, const float* h_dsino,
     if ((s = ck(launch_vlor_count(c->dg, r->events, nevents, r->datos_v, st), "vlor count")) != GF_OK) return done(s);
     if ((s = ck(launch_blankt(c->dg, r->datos_v, s2, r->blankt, st), "blankt")) != GF_OK) return done(s);
   }
-  // STEP 3: initial images (GFIRST.cu:282-288)
-  if ((s = ck(launch_cylinder(c->dg, 1.0f, r->img[0], st), "cylinder")) != GF_OK) return done(s);
-  if ((s = ck(launch_cylinder(c->dg, mode == 1 ? 0.0f : 1.0f, r->img[1], st), "cylinder")) != GF_OK) return done(s);
-  if (mode == 3) {
-    // the triples projection that weights the VLOR split, refreshed subset by subset
-    if ((s = ck(launch_conv_xy(c->dg, r->img[1], nullptr, r->g_fw, r->psf, st), "psf")) != GF_OK) return done(s);
-    if ((s = r->project_all(r->psf, r->proj_t)) != GF_OK) return done(s);
-    if ((s = ck(cudaMemsetAsync(r->datos_v, 0, pl.ndata * sizeof(float), st), "memset")) != GF_OK) return done(s);
-  }
+  if ((s = r->init_images()) != GF_OK) return done(s);
   r->loaded = true;
-  r->iters_done = 0;
-  r->subs_done = 0;
-  r->cur_type = r->cur_sub = 0;
   return done(GF_OK);
+}
+
+gf_status gf_recon_restart(gf_recon* r) {
+  if (!r) return set_error(GF_ERR_ARG, "null reconstruction");
+  if (!r->loaded) return set_error(GF_ERR_STATE, "gf_recon_load has not run");
+  if (r->ntypes == 0) return GF_OK;
+  return r->init_images();
 }
 
 gf_status gf_recon_subiteration(gf_recon* r) {
@@ -242,6 +291,32 @@ gf_status gf_recon_iterate(gf_recon* r, int32_t n) {
   if (r->ntypes == 0) return n == 0 ? GF_OK : set_error(GF_ERR_STATE, "mode 0 has no iterations");
   const int64_t per = (int64_t)r->ntypes * r->ctx->plan.nsub;
   for (int64_t k = 0; k < per * n; k++) GF_TRY(gf_recon_subiteration(r));
+  return GF_OK;
+}
+
+gf_status gf_recon_profile(gf_recon* r, int32_t enable) {
+  if (!r) return set_error(GF_ERR_ARG, "null reconstruction");
+  GF_CK(cudaStreamSynchronize(r->ctx->stream));
+  r->prof = enable != 0;
+  r->ev_used = 0;
+  return GF_OK;
+}
+
+gf_status gf_recon_profile_read(gf_recon* r, int32_t stage, double* total_ms, int64_t* count) {
+  if (!r || !total_ms || !count) return set_error(GF_ERR_ARG, "null argument");
+  if (stage < 0 || stage >= GF_NUM_STAGES) return set_error(GF_ERR_ARG, "no such stage");
+  GF_CK(cudaStreamSynchronize(r->ctx->stream));
+  double tot = 0;
+  int64_t n = 0;
+  for (size_t i = 0; i < r->ev_used; i++) {
+    if (r->evs[i].stage != stage) continue;
+    float ms = 0.f;
+    GF_CK(cudaEventElapsedTime(&ms, r->evs[i].a, r->evs[i].b));
+    tot += ms;
+    n++;
+  }
+  *total_ms = tot;
+  *count = n;
   return GF_OK;
 }
 

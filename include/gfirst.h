@@ -82,6 +82,9 @@ gf_status gf_synchronize(gf_ctx* ctx);
 /* Device memory helpers for callers without a CUDA runtime of their own. */
 gf_status gf_device_alloc(gf_ctx* ctx, size_t bytes, void** d_ptr);
 gf_status gf_device_free(gf_ctx* ctx, void* d_ptr);
+/* Page-locked host memory (fast host<->device copies). */
+gf_status gf_host_alloc(size_t bytes, void** h_ptr);
+gf_status gf_host_free(void* h_ptr);
 /* Synchronous copies on the context's stream. */
 gf_status gf_copy_to_device(gf_ctx* ctx, void* d_dst, const void* h_src, size_t bytes);
 gf_status gf_copy_to_host(gf_ctx* ctx, void* h_dst, const void* d_src, size_t bytes);
@@ -151,6 +154,9 @@ void gf_recon_destroy(gf_recon* r);
  * (GFIRST.cu:207-288).  Mode 0 takes h_image (NVOX floats) instead. */
 gf_status gf_recon_load(gf_recon* r, const float* h_image, const float* h_dsino, const float* h_tsino,
                         const float* h_norm, const int32_t* h_events, int64_t nevents);
+/* Back to the initial images of GFIRST.cu:282-288 (and the initial triples
+ * projection of mode 3) without reloading the data; progress restarts at 0. */
+gf_status gf_recon_restart(gf_recon* r);
 /* Queue n full iterations (every type, every subset), GFIRST.cu:303-564. */
 gf_status gf_recon_iterate(gf_recon* r, int32_t n);
 /* Queue one sub-iteration (one type, one subset) and advance the cursor. */
@@ -164,6 +170,26 @@ gf_status gf_recon_get_image(gf_recon* r, int32_t type, int32_t scaled, float* h
 gf_status gf_recon_get_proj_ref(gf_recon* r, float* h_out);
 /* SINOG_VLOR.raw contents of the last triples sub-iteration (GFIRST.cu:391-394). */
 gf_status gf_recon_get_sinog_vlor(gf_recon* r, float* h_out);
+
+/* ---- measurement (no counterpart in the reference, which only prints a
+ * one-second wall clock, GFIRST.cu:51-52, 572-573) ------------------------- */
+typedef enum gf_stage {
+  GF_STAGE_PSF = 0,       /* forward XY PSF of the current image */
+  GF_STAGE_FP = 1,        /* forward projection (+ fused ratio) */
+  GF_STAGE_VLOR = 2,      /* VLOR split + ratio (mode 3 triples) */
+  GF_STAGE_BP = 3,        /* back projection */
+  GF_STAGE_UPDATE = 4,    /* ratio, XY PSF, axial filter, multiply */
+  GF_STAGE_BILATERAL = 5, /* joint bilateral filter + blend */
+  GF_NUM_STAGES = 6
+} gf_stage;
+/* Record CUDA events around every stage of later sub-iterations (on the
+ * context's stream); enabling clears what was recorded. */
+gf_status gf_recon_profile(gf_recon* r, int32_t enable);
+/* Synchronizes, then returns the summed device time (ms) and the number of
+ * recorded instances of one stage. */
+gf_status gf_recon_profile_read(gf_recon* r, int32_t stage, double* total_ms, int64_t* count);
+/* Kernels this context has launched so far. */
+gf_status gf_kernel_launches(const gf_ctx* ctx, int64_t* n);
 
 /* ---- raw files (GFIRST_CPU_Kernels.cpp:25-142, GFIRST.cu:229-240) --------- */
 /* ReadSinogram_Type (GFIRST_CPU_Kernels.cpp:104-142): int32 file, re-read as

@@ -217,7 +217,15 @@ def test_recon_with_subsets_matches_oracle(gf, mode, nsub):
             continue
         got = r.image(t)
         assert rel(got, want[key]) < IMG_TOL
-        assert rel(got, exact[key]) < IMG_TOL  # error against the FP64 oracle
+        # Error against the FP64 oracle.  The reference's gap rule (an
+        # interpolated ratio < 0 zeroes NUMER and DENOM, GFIRST_GPU_Kernels.cu:157)
+        # is discontinuous where a ratio of exactly 0 meets a -1000 sentinel
+        # row with a weight that is 0 in FP32 and 1e-8 in FP64.  VLOR triples
+        # data are mostly 0, so their DENOM, and the FP32 reference itself,
+        # sit up to ~1e-2 from FP64; the other images stay within 1e-3.
+        fp64_tol = 2e-2 if (mode == 3 and t == 1) else IMG_TOL
+        assert rel(got, exact[key]) < fp64_tol
+        assert abs(rel(got, exact[key]) - rel(want[key], exact[key])) < IMG_TOL
 
 
 def test_recon_small_geometry_mode1_subsets(gf):
