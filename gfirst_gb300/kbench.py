@@ -1,0 +1,55 @@
+"""Kernel micro-benchmark: time one projector stage on a named geometry.
+
+    python -m gfirst_gb300.kbench --op bp|fp|subiter [--geometry preclinical] [--subsets 16] [--reps 5]
+
+Runs a mode-1 reconstruction's stages on synthetic data and reports the
+device time per launch from the library's own stage events.  Small enough to
+run under a profiler (one context, one reconstruction, a few launches).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import numpy as np
+
+import gfirst_gb300 as gf
+
+GEOMS = {"preclinical": gf.Geometry.preclinical, "reference": gf.Geometry.reference, "small": gf.Geometry.small}
+
+
+def run(op: str, geometry: str, nsub: int, reps: int, fp_r: int = 0) -> dict:
+    g = GEOMS[geometry]()
+    ctx = gf.Context(g, nsub=nsub)
+    P, ndata, nvox = gf.sizes(g)
+    rs = np.random.RandomState(5)
+    dsino = np.concatenate([rs.poisson(20.0, ndata), np.zeros(ndata)]).astype(np.float32)
+    norm = rs.uniform(0.85, 1.15, ndata).astype(np.float32)
+    r = gf.Recon(ctx, 1, niter=1)
+    r.load(dsino=dsino, norm=norm)
+    r.subiteration()  # warm-up
+    r.profile(True)
+    for _ in range(reps):
+        r.subiteration()
+    out = {"geometry": geometry, "subsets": nsub, "reps": reps}
+    for name, sid in gf.STAGES.items():
+        tot, n = r.profile_read(sid)
+        if n:
+            out[name + "_ms"] = tot / n
+    r.close()
+    ctx.close()
+    return out
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--op", default="subiter", choices=["bp", "fp", "subiter"])
+    ap.add_argument("--geometry", default="preclinical", choices=sorted(GEOMS))
+    ap.add_argument("--subsets", type=int, default=16)
+    ap.add_argument("--reps", type=int, default=5)
+    a = ap.parse_args()
+    print(json.dumps(run(a.op, a.geometry, a.subsets, a.reps)))
+
+
+if __name__ == "__main__":
+    main()
