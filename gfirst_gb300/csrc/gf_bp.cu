@@ -6,31 +6,41 @@
 // device synchronisation (GFIRST.cu:436-469).
 //
 // GB300 design.  One warp owns one image column (x, y); lane l holds voxels
-// z = l, l+32, ... in registers for the whole subset, so NUMER/DENOM are
-// written once per sub-iteration instead of read and written per view.  For a
-// column and angle the radial bilinear coordinate is fixed; it is computed
-// once per angle into shared memory.  The views are visited in the
-// reference's order (segments outer, angles inner) and every coordinate is
-// computed with the reference's rounding, so each voxel's sums are the
-// reference's sums bit for bit.  The (corr, calib) pairs of a view sit in
-// radial-major rows, so the 32 lanes of a warp (consecutive z, hence
-// consecutive rows) read contiguous 8-byte pairs; the padded rows around each
-// segment stand in for the clamp / -1000 texels at the plane-range edges.
+// z = l, l+32, ... and their (NUMER, DENOM) pairs in registers for the whole
+// subset, so the volumes are written once per sub-iteration.  For a column
+// and an angle the radial coordinate is fixed, so per (segment, angle) view:
+//  (1) the warp interpolates every plane row of the view radially once
+//      (lanes along rows: coalesced 8-byte (corr, calib) loads from the
+//      radial-major layout) into warp-private shared memory;
+//  (2) each voxel interpolates between two of those rows along z.
+// That is one radial interpolation per row instead of two per voxel; lane
+// chunks with no voxel inside the segment's plane range are skipped.
+// (corr, calib) are processed as packed FP32 pairs (sm_100+ f32x2 FMA/add),
+// each element rounded as the scalar operation would be.  Views are visited
+// in the reference's order (segments outer, angles inner) with the
+// reference's coordinate rounding, so every voxel's sums are the reference's
+// sums bit for bit.
 #include "gf_kernels.h"
 
 namespace gf {
 
+__device__ __forceinline__ float2 lerp2(float2 a, float2 b, float2 w) {
+  return __ffma2_rn(w, __fadd2_rn(b, make_float2(-a.x, -a.y)), a);
+}
+
 template <int Q>
-__global__ void __launch_bounds__(256) bp_kernel(const BpArgs a) {
-  extern __shared__ int4 bcache[];  // [warps per block][na]
+__global__ void __launch_bounds__(256) bp_kernel(const BpArgs a, int rmax) {
+  extern __shared__ __align__(16) unsigned char smraw[];
   const DevGeom& g = a.g;
+  const int nwarps = blockDim.x >> 5;
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int colidx = blockIdx.x * (blockDim.x >> 5) + wib;
+  const int colidx = blockIdx.x * nwarps + wib;
   if (colidx >= g.res * g.res) return;  // whole warp
   const int iy = colidx / g.res, ix = colidx - iy * g.res;
-  int4* my = bcache + wib * a.na;
+  int4* my = reinterpret_cast<int4*>(smraw) + wib * a.na;
+  float2* rows = reinterpret_cast<float2*>(reinterpret_cast<int4*>(smraw) + nwarps * a.na) + wib * rmax;
 
-  // GFIRST_GPU_Kernels.cu:136-147
+  // per angle: radial texels, weight and yrot (GFIRST_GPU_Kernels.cu:136-147)
   const float xv = __fsub_rn((float)ix, g.resm), yv = __fsub_rn((float)iy, g.resm);
   for (int tl = lane; tl < a.na; tl += 32) {
     const float2 sc = g.trig[subset_angle(g, a.subset, tl)];
@@ -46,39 +56,54 @@ __global__ void __launch_bounds__(256) bp_kernel(const BpArgs a) {
   }
   __syncwarp();
 
-  float na[Q], da[Q];
+  float fiz[Q];
+  float2 acc[Q];
 #pragma unroll
-  for (int q = 0; q < Q; q++) na[q] = da[q] = 0.f;
+  for (int q = 0; q < Q; q++) {
+    fiz[q] = (float)(lane + 32 * q);
+    acc[q] = make_float2(0.f, 0.f);
+  }
 
   for (int s = 0; s < g.nseg; s++) {
     const DevSeg sg = g.seg[s];
     const float zlo = (float)sg.zmin, zhi = (float)(g.nzs - sg.zmin);
-    const int roff = sg.blk + 1 - sg.zmin;
+    const int zm1 = sg.zmin - 1;
+    const int nrow = sg.nplanes + 2;
     for (int tl = 0; tl < a.na; tl++) {
       const int4 e = my[tl];
-      const float al = __int_as_float(e.z);
+      const float2 al2 = make_float2(__int_as_float(e.z), __int_as_float(e.z));
       const float t = __fmul_rn(__int_as_float(e.w), sg.fz);  // yrot*fz
-      const float2* p0 = a.corrcal + e.x + roff;
-      const float2* p1 = a.corrcal + e.y + roff;
+      const float2* p0 = a.corrcal + e.x + sg.blk;
+      const float2* p1 = a.corrcal + e.y + sg.blk;
+      float2 c0[Q + 1], c1[Q + 1];
+#pragma unroll
+      for (int k = 0; k <= Q; k++) {
+        const int r = lane + 32 * k;
+        if (r < nrow) {
+          c0[k] = __ldg(p0 + r);
+          c1[k] = __ldg(p1 + r);
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int k = 0; k <= Q; k++) {
+        const int r = lane + 32 * k;
+        if (r < nrow) rows[r] = lerp2(c0[k], c1[k], al2);
+      }
+      __syncwarp();
 #pragma unroll
       for (int q = 0; q < Q; q++) {
-        const int iz = lane + 32 * q;
         // z = float(iz) + yrot*fz + 0.5f, GFIRST_GPU_Kernels.cu:148
-        const float z = __fadd_rn(__fadd_rn((float)iz, t), 0.5f);
-        if (iz < g.nzs && z >= zlo && z < zhi) {
+        const float z = __fadd_rn(__fadd_rn(fiz[q], t), 0.5f);
+        const bool in = (lane + 32 * q < g.nzs) && z >= zlo && z < zhi;
+        if (__any_sync(0xffffffffu, in) && in) {
           const float zb = __fsub_rn(z, 0.5f);
           const float fz = floorf(zb);
-          const int j = (int)fz;
+          const int j = (int)fz - zm1;
           const float be = __fsub_rn(zb, fz);
-          const float2 t00 = __ldg(p0 + j), t10 = __ldg(p1 + j);
-          const float2 t01 = __ldg(p0 + j + 1), t11 = __ldg(p1 + j + 1);
-          const float c = lerp_rn(lerp_rn(t00.x, t10.x, al), lerp_rn(t01.x, t11.x, al), be);
-          const float k = lerp_rn(lerp_rn(t00.y, t10.y, al), lerp_rn(t01.y, t11.y, al), be);
+          const float2 v = lerp2(rows[j], rows[j + 1], make_float2(be, be));
           // GFIRST_GPU_Kernels.cu:157: a negative interpolated value (a gap) zeroes both
-          if (!(k < 0.f || c < 0.f)) {
-            na[q] = __fadd_rn(na[q], c);
-            da[q] = __fadd_rn(da[q], k);
-          }
+          if (!(v.y < 0.f || v.x < 0.f)) acc[q] = __fadd2_rn(acc[q], v);
         }
       }
     }
@@ -88,17 +113,18 @@ __global__ void __launch_bounds__(256) bp_kernel(const BpArgs a) {
 #pragma unroll
   for (int q = 0; q < Q; q++) {
     const int iz = lane + 32 * q;
-    no[iz] = iz < g.nzs ? na[q] : 0.f;
-    dO[iz] = iz < g.nzs ? da[q] : 0.f;
+    no[iz] = iz < g.nzs ? acc[q].x : 0.f;
+    dO[iz] = iz < g.nzs ? acc[q].y : 0.f;
   }
 }
 
 cudaError_t launch_bp(const BpArgs& a, cudaStream_t st) {
   const int warps = 8;
   const int Q = a.g.nzp / 32;
-  size_t smem = (size_t)warps * a.na * sizeof(int4);
+  const int rmax = a.g.nzs + 2;
+  size_t smem = (size_t)warps * (a.na * sizeof(int4) + rmax * sizeof(float2));
   dim3 grid((a.g.res * a.g.res + warps - 1) / warps);
-  void (*k)(BpArgs) = nullptr;
+  void (*k)(BpArgs, int) = nullptr;
   switch (Q) {
     case 1: k = bp_kernel<1>; break;
     case 2: k = bp_kernel<2>; break;
@@ -114,7 +140,7 @@ cudaError_t launch_bp(const BpArgs& a, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  k<<<grid, warps * 32, smem, st>>>(a);
+  k<<<grid, warps * 32, smem, st>>>(a, rmax);
   return cudaGetLastError();
 }
 
