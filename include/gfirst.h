@@ -129,6 +129,26 @@ gf_status gf_vlor_count(gf_ctx* ctx, const int32_t* d_events, int64_t nevents, f
 gf_status gf_vlor_split(gf_ctx* ctx, const int32_t* d_events, int64_t nevents, const float* d_proj,
                         const float* d_blankt, float* d_out);
 
+/* ---- forward projection without device allocation ------------------------ */
+/* Size of the fixed device scratch behind gf_forward_project_noalloc. */
+#define GF_NOALLOC_SCRATCH_BYTES (16u << 20)
+/* Forward projection of one subset, as gf_forward_project, for callers that
+ * cannot allocate device memory (a host that owns the whole device memory
+ * map, an embedding framework with its own pool, code where an allocation
+ * would stall or be refused).  No counterpart in the reference.  Needs no
+ * context and calls no cudaMalloc/cudaFree: its scratch (the image
+ * transposed to z-fastest order plus the geometry tables) lives in one
+ * file-scope device array of GF_NOALLOC_SCRATCH_BYTES bytes, held by every
+ * GPU that loads the library until the process exits.  Geometries whose
+ * scratch exceeds it (image RES*RES*NZS padded to 32 slices, about 4.1 M
+ * voxels) are rejected with GF_ERR_ARG.  Runs on the current device and on
+ * `cuda_stream` (NULL: the legacy default stream).  The first call on a
+ * device looks up the array's device address; make that call before any
+ * stream capture.  All calls share the array: calls whose work overlaps on
+ * the GPU race. */
+gf_status gf_forward_project_noalloc(const gf_geometry* g, int32_t nsubsets, int32_t subset, const float* d_image,
+                                     float* d_proj, void* cuda_stream);
+
 /* ---- whole reconstruction -------------------------------------------------- */
 /* The four CLI modes of GFIRST.cu:588-617: 0 projection of an image,
  * 1 doubles sinogram + normalization, 2 doubles + triples sinograms,
