@@ -228,6 +228,9 @@ class Context:
     def vlor_count(self, ev, nev, cnt) -> None:
         _ck(lib().gf_vlor_count(self.h, ev.p, ctypes.c_int64(nev), cnt.p))
 
+    def vlor_from_endpoints(self, lors, nev, events) -> None:
+        _ck(lib().gf_vlor_from_endpoints(self.h, lors.p, ctypes.c_int64(nev), events.p))
+
     def vlor_split(self, ev, nev, proj, blankt, out) -> None:
         _ck(lib().gf_vlor_split(self.h, ev.p, ctypes.c_int64(nev), proj.p, blankt.p, out.p))
 
@@ -312,6 +315,20 @@ def read_vlor(path) -> np.ndarray:
     out = np.zeros(max(1, n.value) * 2, np.int32)
     _ck(lib().gf_read_vlor(str(path).encode(), _ptr(out), ctypes.byref(n)))
     return out[: 2 * n.value].reshape(-1, 2)
+
+
+def bin_endpoints(g: Geometry, bin_index: int) -> np.ndarray:
+    out = np.empty(6, np.float32)
+    _ck(lib().gf_bin_endpoints(ctypes.byref(g.c()), ctypes.c_int64(bin_index), _ptr(out)))
+    return out
+
+
+def read_vlor_endpoints(path) -> np.ndarray:
+    n = ctypes.c_int64()
+    _ck(lib().gf_read_vlor_endpoints(str(path).encode(), None, ctypes.byref(n)))
+    out = np.zeros(max(1, n.value) * 12, np.float32)
+    _ck(lib().gf_read_vlor_endpoints(str(path).encode(), _ptr(out), ctypes.byref(n)))
+    return out[: 12 * n.value].reshape(-1, 12)
 
 
 def read_image(path, nvox: int) -> np.ndarray:

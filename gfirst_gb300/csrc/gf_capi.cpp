@@ -331,6 +331,46 @@ gf_status gf_copy_to_host(gf_ctx* c, void* h, const void* d, size_t bytes) {
   return GF_OK;
 }
 
+// ---------------------------------------------------------------- VLOR endpoints
+gf_status gf_bin_endpoints(const gf_geometry* gg, int64_t bin, float* out6) {
+  Geom geo;
+  if (!to_geom(gg, &geo) || !out6) return set_error(GF_ERR_ARG, "null argument");
+  Plan p;
+  std::string err;
+  if (!make_plan(geo, 1, &p, &err)) return set_error(GF_ERR_GEOMETRY, err);
+  if (bin < 0 || bin >= p.ndata) return set_error(GF_ERR_ARG, "bin out of range");
+  const int64_t row = bin / ((int64_t)geo.nrad * geo.nang);
+  const int t = (int)((bin / geo.nrad) % geo.nang), ird = (int)(bin % geo.nrad);
+  int s = 0;
+  while (s + 1 < geo.nseg && p.seg[s + 1].acc <= row) s++;
+  const Seg& sg = p.seg[s];
+  const int iz0 = (int)(row - sg.acc) + sg.zmin;
+  // the forward projector's ray of this bin (GFIRST_GPU_Kernels.cu:75-96), in mm
+  const double vx = (double)(geo.fov / (float)geo.res), hs = 0.5 * (double)geo.pitch;
+  const double sn = p.sinv[t], cs = p.cosv[t];
+  const double x0 = (double)p.fx_fp * ((double)ird - (double)p.radm) * vx;
+  const double cx = x0 * cs, cy = x0 * sn;
+  const double R = 0.5 * (double)geo.diam;
+  const double h2 = R * R - x0 * x0;
+  if (h2 <= 0.0) return set_error(GF_ERR_ARG, "bin's line of response misses the detector ring");
+  const double lam = std::sqrt(h2) / vx;  // voxel steps from the closest point to the ring
+  for (int k = 0; k < 2; k++) {
+    const double l = k == 0 ? -lam : lam;
+    const double zt = (double)iz0 + 0.5 + l * (double)sg.dz;
+    out6[3 * k + 0] = (float)(cx + l * vx * sn);
+    out6[3 * k + 1] = (float)(cy - l * vx * cs);
+    out6[3 * k + 2] = (float)((zt - 0.5 * geo.nzs) * hs);
+  }
+  return GF_OK;
+}
+
+gf_status gf_vlor_from_endpoints(gf_ctx* c, const float* d_lors, int64_t n, int32_t* d_events) {
+  if (!c || (!d_lors && n) || (!d_events && n) || n < 0) return set_error(GF_ERR_ARG, "bad argument");
+  const float vx = c->plan.g.fov / (float)c->plan.g.res, hs = 0.5f * c->plan.g.pitch;
+  GF_LAUNCH(c, launch_vlor_endpoints(c->dg, d_lors, n, vx, hs, d_events, c->stream));
+  return GF_OK;
+}
+
 // ---------------------------------------------------------------- operators
 static gf_status check_subset(const gf_ctx* c, int32_t subset) {
   if (!c) return set_error(GF_ERR_ARG, "null context");

@@ -11,6 +11,8 @@
 // reference fixes at compile time:
 //   --geometry res,nzs,nrad,nang,span,nseg,pitch,diam,fov   (default GFIRST.h)
 //   --subsets S  --iterations N  --write-every K  --device D
+//   --vlor-endpoints   the VLOR file holds two LORs of float32 endpoints per
+//                      event (gf_read_vlor_endpoints) instead of int32 bins
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -26,7 +28,7 @@ static int usage() {
   printf("3 Inputs --> Reconstruction Doubles & Triples [Input = Sinog_Doubles + Sinog_Triples + Sinog_Normalization] \n");
   printf("4 Inputs --> VLOR reconstruction [Input = Sinog_Doubles + Sinog_Triples + Sinog_Normalization + Vlor_file] \n");
   printf("options: --geometry res,nzs,nrad,nang,span,nseg,pitch,diam,fov --subsets S --iterations N "
-         "--write-every K --device D\n");
+         "--write-every K --device D --vlor-endpoints\n");
   return 0;
 }
 
@@ -39,6 +41,7 @@ int main(int argc, char** argv) {
   gf_geometry g;
   gf_geometry_reference(&g);
   int nsub = 1, niter = -1, every = 20, device = 0;
+  bool vlor_endpoints = false;
   std::vector<std::string> files;
   for (int i = 1; i < argc; i++) {
     std::string a = argv[i];
@@ -64,6 +67,8 @@ int main(int argc, char** argv) {
       every = atoi(val("--write-every"));
     } else if (a == "--device") {
       device = atoi(val("--device"));
+    } else if (a == "--vlor-endpoints") {
+      vlor_endpoints = true;
     } else if (a == "-h" || a == "--help") {
       return usage();
     } else {
@@ -101,11 +106,26 @@ int main(int argc, char** argv) {
       tsino.resize(2 * ndata);
       if (gf_read_sinogram(files[1].c_str(), ndata, tsino.data()) != GF_OK) printf("Sinogram Not Found!\n");
     }
-    if (mode == 3) {
+    if (mode == 3 && !vlor_endpoints) {
       printf("Reading VLOR file \n");
       if ((st = gf_read_vlor(files[3].c_str(), nullptr, &nev)) != GF_OK) return die("read VLOR", st);
       ev.resize(2 * (size_t)nev + 2);
       if ((st = gf_read_vlor(files[3].c_str(), ev.data(), &nev)) != GF_OK) return die("read VLOR", st);
+    } else if (mode == 3) {
+      printf("Reading VLOR file (LOR endpoints) \n");
+      if ((st = gf_read_vlor_endpoints(files[3].c_str(), nullptr, &nev)) != GF_OK) return die("read VLOR", st);
+      std::vector<float> lors(12 * (size_t)nev + 12);
+      if ((st = gf_read_vlor_endpoints(files[3].c_str(), lors.data(), &nev)) != GF_OK) return die("read VLOR", st);
+      ev.resize(2 * (size_t)nev + 2);
+      void *dl = nullptr, *de = nullptr;
+      if ((st = gf_device_alloc(ctx, lors.size() * sizeof(float), &dl)) != GF_OK) return die("alloc", st);
+      if ((st = gf_device_alloc(ctx, ev.size() * sizeof(int32_t), &de)) != GF_OK) return die("alloc", st);
+      if ((st = gf_copy_to_device(ctx, dl, lors.data(), lors.size() * sizeof(float))) != GF_OK) return die("copy", st);
+      if ((st = gf_vlor_from_endpoints(ctx, static_cast<const float*>(dl), nev, static_cast<int32_t*>(de))) != GF_OK)
+        return die("VLOR endpoints", st);
+      if ((st = gf_copy_to_host(ctx, ev.data(), de, ev.size() * sizeof(int32_t))) != GF_OK) return die("copy", st);
+      gf_device_free(ctx, dl);
+      gf_device_free(ctx, de);
     }
     double sumd = 0, sumdbg = 0;
     for (int64_t i = 0; i < ndata; i++) {

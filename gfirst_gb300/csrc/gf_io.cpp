@@ -93,6 +93,30 @@ gf_status gf_read_vlor(const char* path, int32_t* h_events, int64_t* nevents) {
   return GF_OK;
 }
 
+// VLOR events as two LORs of endpoints each: 48-byte records of 12 float32.
+gf_status gf_read_vlor_endpoints(const char* path, float* h_lors, int64_t* nevents) {
+  if (!path || !nevents) return set_error(GF_ERR_ARG, "bad argument");
+  FILE* f = fopen(path, "rb");
+  if (!f) return set_error(GF_ERR_IO, std::string("VLOR file Not Found: ") + path);
+  long bytes = file_size(f);
+  const int64_t n = bytes > 0 ? bytes / 48 : 0;
+  if (!h_lors) {
+    fclose(f);
+    *nevents = n;
+    return GF_OK;
+  }
+  if (*nevents < n) {
+    fclose(f);
+    *nevents = n;
+    return set_error(GF_ERR_ARG, "event buffer too small");
+  }
+  size_t got = n ? fread(h_lors, 48, (size_t)n, f) : 0;
+  fclose(f);
+  if ((int64_t)got != n) return set_error(GF_ERR_IO, std::string("short read: ") + path);
+  *nevents = n;
+  return GF_OK;
+}
+
 // WriteImage, GFIRST_CPU_Kernels.cpp:25-33.
 gf_status gf_write_raw(const char* path, const float* h_data, int64_t n) {
   if (!path || (!h_data && n) || n < 0) return set_error(GF_ERR_ARG, "bad argument");

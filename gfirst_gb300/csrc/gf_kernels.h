@@ -73,4 +73,7 @@ cudaError_t launch_blankt(const DevGeom& g, const float* cnt, const float* tsino
 cudaError_t launch_vlor_split(const DevGeom& g, const int32_t* ev, long long nev, const float* proj,
                               const float* blankt, float* out, cudaStream_t st);
 
+cudaError_t launch_vlor_endpoints(const DevGeom& g, const float* lors, long long n, float vx, float hs, int32_t* ev,
+                                  cudaStream_t st);
+
 }  // namespace gf

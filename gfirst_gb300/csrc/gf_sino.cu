@@ -261,4 +261,66 @@ cudaError_t launch_vlor_split(const DevGeom& g, const int32_t* ev, long long nev
   return cudaGetLastError();
 }
 
+// ---- VLOR events given as LOR endpoints -----------------------------------
+// One LOR (x1,y1,z1,x2,y2,z2 in mm; x/y about the axis, z about the axial
+// centre) -> 0-based sinogram bin, or -1.  Inverse of gf_bin_endpoints.
+__device__ long long lor_bin(const DevGeom& g, const float* e, float vx, float hs, float pi_ref) {
+  const float dx = e[3] - e[0], dy = e[4] - e[1], dzm = e[5] - e[2];
+  const float L = sqrtf(dx * dx + dy * dy);
+  if (!(L > 0.f)) return -1;
+  float ux = dx / L, uy = dy / L, sgn = 1.f;
+  // direction (sin t, -cos t) with t in (0, pi]
+  float th = atan2f(ux, -uy);
+  if (th <= 0.f) {
+    th += pi_ref;
+    sgn = -sgn;
+  }
+  int t = __float2int_rn((pi_ref - th) * (float)g.nang / pi_ref);
+  if (t >= g.nang) {
+    t -= g.nang;
+    sgn = -sgn;
+  }
+  if (t < 0) t += g.nang;
+  const float2 sc = g.trig[t];  // (sin, cos)
+  ux = sgn * (dx / L);
+  uy = sgn * (dy / L);
+  const float x0mm = e[0] * sc.y + e[1] * sc.x;
+  const int ird = __float2int_rn(x0mm / (vx * g.fx_fp) + g.radm);
+  if (ird < 0 || ird >= g.nrad) return -1;
+  const float slope = sgn * dzm / L * vx / hs;  // slices per voxel step along the ray
+  int best = -1;
+  float bd = 3.0e38f;
+  for (int s = 0; s < g.nseg; s++) {
+    const float d = fabsf(g.seg[s].dz - slope);
+    if (d < bd) {
+      bd = d;
+      best = s;
+    }
+  }
+  const DevSeg sg = g.seg[best];
+  const float cx = x0mm * sc.y, cy = x0mm * sc.x;
+  const float lam1 = ((e[0] - cx) * ux + (e[1] - cy) * uy) / vx;
+  const float z0 = e[2] / hs + 0.5f * (float)g.nzs - lam1 * sg.dz;  // texel z at the closest point
+  const int iz0 = __float2int_rn(z0 - 0.5f);
+  if (iz0 < sg.zmin || iz0 >= g.nzs - sg.zmin) return -1;
+  return ((long long)(iz0 - sg.zmin) + sg.acc) * ((long long)g.nrad * g.nang) + (long long)t * g.nrad + ird;
+}
+
+__global__ void vlor_endpoints_kernel(const DevGeom g, const float* __restrict__ lors, long long n, float vx, float hs,
+                                      float pi_ref, int32_t* __restrict__ ev) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int k = 0; k < 2; k++) {
+    const long long b = lor_bin(g, lors + 12 * i + 6 * k, vx, hs, pi_ref);
+    ev[2 * i + k] = (int32_t)(b + 1);  // 1-based; 0 = rejected, as the reference rejects i <= 0
+  }
+}
+
+cudaError_t launch_vlor_endpoints(const DevGeom& g, const float* lors, long long n, float vx, float hs, int32_t* ev,
+                                  cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  vlor_endpoints_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, lors, n, vx, hs, 3.1415926f, ev);
+  return cudaGetLastError();
+}
+
 }  // namespace gf

@@ -149,6 +149,23 @@ gf_status gf_vlor_split(gf_ctx* ctx, const int32_t* d_events, int64_t nevents, c
 gf_status gf_forward_project_noalloc(const gf_geometry* g, int32_t nsubsets, int32_t subset, const float* d_image,
                                      float* d_proj, void* cuda_stream);
 
+/* ---- VLOR events as LOR endpoints (no counterpart in the reference, whose
+ * VLOR file holds int32 pairs of 1-based bins, GFIRST.cu:213-240) ---------- */
+/* Endpoints in mm of the line of response of sinogram bin `bin` (0-based):
+ * out6 = (x1,y1,z1,x2,y2,z2), both ends on the detector ring (radius
+ * DIAM_DET/2), x/y about the scanner axis, z about the centre of the axial
+ * field of view.  The line is the one the forward projector samples for that
+ * bin (GFIRST_GPU_Kernels.cu:75-96). */
+gf_status gf_bin_endpoints(const gf_geometry* g, int64_t bin, float* out6);
+/* Converts n VLOR events given as two LORs each (12 float32 per event:
+ * endpoints of the first candidate LOR, then of the second) to the
+ * reference's event format (int32 pairs of 1-based bins; 0 where a LOR falls
+ * outside the sinogram).  Inverse of gf_bin_endpoints at bin centres: angle
+ * from the in-plane direction, radial bin from the distance to the axis,
+ * segment from the axial slope, plane from the axial position at the point
+ * closest to the axis. */
+gf_status gf_vlor_from_endpoints(gf_ctx* ctx, const float* d_lors, int64_t nevents, int32_t* d_events);
+
 /* ---- whole reconstruction -------------------------------------------------- */
 /* The four CLI modes of GFIRST.cu:588-617: 0 projection of an image,
  * 1 doubles sinogram + normalization, 2 doubles + triples sinograms,
@@ -222,6 +239,10 @@ gf_status gf_read_image(const char* path, int64_t nvox, float* h_out);
  * while(!feof) loop over the last record.  With h_events NULL only the count
  * is returned; otherwise up to *nevents pairs are written. */
 gf_status gf_read_vlor(const char* path, int32_t* h_events, int64_t* nevents);
+/* VLOR events as LOR endpoints: 48-byte records of 12 float32 (see
+ * gf_vlor_from_endpoints); trailing bytes of a partial record are ignored.
+ * With h_lors NULL only the count is returned. */
+gf_status gf_read_vlor_endpoints(const char* path, float* h_lors, int64_t* nevents);
 /* WriteImage (GFIRST_CPU_Kernels.cpp:25-33). */
 gf_status gf_write_raw(const char* path, const float* h_data, int64_t n);
 

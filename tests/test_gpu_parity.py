@@ -320,3 +320,46 @@ def test_preclinical_properties(gf, c2):
     ctx.back_project(ones_s, ones_s, 9, numer, denom)
     n, d = numer.download(), denom.download()
     assert np.array_equal(n, d) and n.max() > 0  # identical channels give identical sums
+
+
+# ---------------------------------------------------------------- VLOR as LOR endpoints
+def endpoint_events(gf, g, pairs):
+    return np.stack([np.concatenate([gf.bin_endpoints(g, int(a)), gf.bin_endpoints(g, int(b))]) for a, b in pairs])
+
+
+@pytest.mark.parametrize("name", ["tiny", "preclinical"])
+def test_vlor_endpoints_round_trip_at_bin_centres(gf, name):
+    g = gf.Geometry(*inputs.GEOMS["tiny"]) if name == "tiny" else gf.Geometry.preclinical()
+    ctx = gf.Context(g)
+    rs = np.random.RandomState(6)
+    bins = np.arange(ctx.ndata) if name == "tiny" else rs.randint(0, ctx.ndata, 20000)
+    pairs = np.stack([bins, rs.permutation(bins)], axis=1)
+    lors = endpoint_events(gf, g, pairs).astype(np.float32)
+    dl, de = ctx.put(lors), ctx.array(2 * len(pairs), np.int32)
+    ctx.vlor_from_endpoints(dl, len(pairs), de)
+    got = de.download().reshape(-1, 2)
+    assert np.array_equal(got, pairs + 1)
+
+
+def test_mode3_from_endpoint_events_equals_bin_events(gf):
+    name = "tiny"
+    geo = inputs.GEOMS[name]
+    g = gf.Geometry(*geo)
+    d = parsed(name)
+    ndata, _ = inputs.sizes(name)
+    ev = d["events"]
+    ev = ev[(ev >= 1).all(axis=1) & (ev <= ndata).all(axis=1)]
+    ctx = gf.Context(g, nsub=2)
+    lors = endpoint_events(gf, g, ev - 1).astype(np.float32)
+    dl, de = ctx.put(lors), ctx.array(2 * len(ev), np.int32)
+    ctx.vlor_from_endpoints(dl, len(ev), de)
+    ev2 = de.download().reshape(-1, 2)
+    assert np.array_equal(ev2, ev)
+    imgs = []
+    for events in (ev, ev2):
+        r = gf.Recon(ctx, 3, niter=2)
+        r.load(dsino=d["dsino"], tsino=d["tsino"], norm=d["norm"], events=events)
+        r.iterate(2)
+        imgs.append(r.image(1))
+        r.close()
+    assert rel(imgs[0], imgs[1]) < 1e-6

@@ -148,3 +148,22 @@ def test_image_reader(gf, tmp_path):
 def test_cli_usage_without_arguments(gf):
     out = subprocess.run([str(gf.CLI_PATH)], capture_output=True, text=True)
     assert out.returncode == 0 and "1 Input  --> Projection" in out.stdout
+
+
+@pytest.mark.parametrize("geo", [inputs.GEOMS["tiny"], (128, 159, 128, 160, 3, 53, 1.6, 165.7758, 100.0)])
+def test_bin_endpoints_lie_on_the_detector_ring(gf, geo):
+    g = gf.Geometry(*geo)
+    _, ndata, _ = gf.sizes(g)
+    rs = np.random.RandomState(0)
+    for b in rs.randint(0, ndata, size=200):
+        e = gf.bin_endpoints(g, int(b)).astype(np.float64)
+        r1, r2 = np.hypot(e[0], e[1]), np.hypot(e[3], e[4])
+        assert abs(r1 - g.diam / 2) < 1e-3 and abs(r2 - g.diam / 2) < 1e-3
+        assert abs(e[2]) < g.nzs * g.pitch and abs(e[5]) < g.nzs * g.pitch
+
+
+def test_vlor_endpoint_reader(gf, tmp_path):
+    lors = np.arange(12 * 3, dtype=np.float32).reshape(3, 12)
+    p = tmp_path / "v.raw"
+    p.write_bytes(lors.tobytes() + b"\x00" * 20)
+    assert np.array_equal(gf.read_vlor_endpoints(p), lors)
