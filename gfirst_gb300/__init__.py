@@ -83,6 +83,7 @@ def _load() -> ctypes.CDLL:
         getattr(lib, name)
     lib.gf_destroy.restype = None
     lib.gf_recon_destroy.restype = None
+    lib.gf_batch_destroy.restype = None
     lib.gf_copy_to_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
     lib.gf_copy_to_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
     lib.gf_device_alloc.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
@@ -202,6 +203,11 @@ class Context:
         _ck(lib().gf_kernel_launches(self.h, ctypes.byref(n)))
         return n.value
 
+    def tune(self) -> dict:
+        r, lc, w = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _ck(lib().gf_tune(self.h, ctypes.byref(r), ctypes.byref(lc), ctypes.byref(w)))
+        return {"fp_run": r.value, "fp_chunk": lc.value, "bp_warps": w.value}
+
     # operators on device arrays (reference file layouts)
     def forward_project(self, img: DeviceArray, subset: int, proj: DeviceArray) -> None:
         _ck(lib().gf_forward_project(self.h, img.p, subset, proj.p))
@@ -301,6 +307,34 @@ class Recon:
         out = np.empty(self.ctx.ndata, np.float32)
         _ck(lib().gf_recon_get_sinog_vlor(self.h, _ptr(out)))
         return out
+
+
+class Batch:
+    """gf_batch: loaded reconstructions advancing together, optionally from a CUDA graph."""
+
+    def __init__(self, recons):
+        self.recons = list(recons)
+        arr = (ctypes.c_void_p * len(self.recons))(*[r.h.value for r in self.recons])
+        h = ctypes.c_void_p()
+        _ck(lib().gf_batch_create(len(self.recons), arr, ctypes.byref(h)))
+        self.h = h
+
+    def iterate(self, n: int = 1, graph: bool = True) -> None:
+        _ck(lib().gf_batch_iterate(self.h, n, int(graph)))
+
+    def sync(self) -> None:
+        _ck(lib().gf_batch_synchronize(self.h))
+
+    def close(self) -> None:
+        if self.h:
+            lib().gf_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def read_sinogram(path, ndata: int):

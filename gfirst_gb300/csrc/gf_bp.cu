@@ -118,8 +118,8 @@ __global__ void __launch_bounds__(256) bp_kernel(const BpArgs a, int rmax) {
   }
 }
 
-cudaError_t launch_bp(const BpArgs& a, cudaStream_t st) {
-  const int warps = 8;
+cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st) {
+  if (warps < 1 || warps > 8) return cudaErrorInvalidValue;
   const int Q = a.g.nzp / 32;
   const int rmax = a.g.nzs + 2;
   size_t smem = (size_t)warps * (a.na * sizeof(int4) + rmax * sizeof(float2));

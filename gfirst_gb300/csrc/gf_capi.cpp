@@ -240,7 +240,7 @@ gf_status gf_create(const gf_geometry* g, int32_t nsubsets, int32_t device, gf_c
   if ((st = c->alloc_t(segs.size(), &c->d_seg)) != GF_OK) return fail(st);
   if ((st = c->alloc_t(trig.size(), &c->d_trig)) != GF_OK) return fail(st);
   if ((st = c->alloc_t(rowmap.size(), &c->d_rowmap)) != GF_OK) return fail(st);
-  if ((st = c->alloc_t(runs.size(), &c->d_runs)) != GF_OK) return fail(st);
+  if ((st = c->alloc_t(512, &c->d_runs)) != GF_OK) return fail(st);  // room for any schedule (<= 512 threads)
   cudaMemcpy(c->d_seg, segs.data(), segs.size() * sizeof(DevSeg), cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_trig, trig.data(), trig.size() * sizeof(float2), cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_rowmap, rowmap.data(), rowmap.size() * sizeof(int2), cudaMemcpyHostToDevice);
@@ -411,7 +411,7 @@ gf_status gf_back_project(gf_ctx* c, const float* d_corr, const float* d_calib, 
   const int na = c->plan.sub_nang[subset];
   GF_LAUNCH(c, launch_corrcal_from_file(c->dg, c->d_rowmap, subset, na, d_corr, d_calib, c->s_cc, c->stream));
   BpArgs b{c->dg, subset, na, c->s_cc, c->s_numer, c->s_denom};
-  GF_LAUNCH(c, launch_bp(b, c->stream));
+  GF_LAUNCH(c, launch_bp(b, c->bp_warps, c->stream));
   GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_numer, 1.f, 0, d_numer, c->stream));
   GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_denom, 1.f, 0, d_denom, c->stream));
   return GF_OK;
@@ -433,8 +433,8 @@ gf_status gf_image_update(gf_ctx* c, float* d_image, const float* d_numer, const
   GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_denom, c->s_denom, c->stream));
   GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_image, c->s_img, c->stream));
   GF_LAUNCH(c, launch_conv_xy(c->dg, c->s_numer, c->s_denom, gauss9(psf_bw), c->s_img2, c->stream));
-  GF_LAUNCH(c, launch_zfilter_update(c->dg, c->s_img2, c->s_img, gauss5(), c->s_numer, c->stream));
-  GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_numer, 1.f, 0, d_image, c->stream));
+  GF_LAUNCH(c, launch_zfilter_update(c->dg, c->s_img2, gauss5(), c->s_img, c->stream));
+  GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_img, 1.f, 0, d_image, c->stream));
   return GF_OK;
 }
 

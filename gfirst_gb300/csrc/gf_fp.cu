@@ -59,8 +59,8 @@ __global__ void __launch_bounds__(512) fp_kernel(const FpArgs a) {
   const int npad = cw - NZS;
   for (int lb = g.lam0; lb <= g.lam1; lb += lc) {
     const int nl = min(lc, g.lam1 - lb + 1);
-    if (tid < nl) {
-      const float fl = (float)(lb + tid);
+    for (int l = tid; l < nl; l += nt) {
+      const float fl = (float)(lb + l);
       const float x = __fadd_rn(xc, __fmul_rn(fl, dx));
       const float y = __fadd_rn(yc, __fmul_rn(fl, dy));
       const float xb = __fsub_rn(x, 0.5f), yb = __fsub_rn(y, 0.5f);
@@ -68,8 +68,8 @@ __global__ void __launch_bounds__(512) fp_kernel(const FpArgs a) {
       const int i = (int)fx, j = (int)fy;
       const int i0 = clampi(i, 0, RES - 1), i1 = clampi(i + 1, 0, RES - 1);
       const int j0 = clampi(j, 0, RES - 1), j1 = clampi(j + 1, 0, RES - 1);
-      offs[tid] = make_int4((j0 * RES + i0) * NZP, (j0 * RES + i1) * NZP, (j1 * RES + i0) * NZP, (j1 * RES + i1) * NZP);
-      wts[tid] = make_float2(__fsub_rn(xb, fx), __fsub_rn(yb, fy));
+      offs[l] = make_int4((j0 * RES + i0) * NZP, (j0 * RES + i1) * NZP, (j1 * RES + i0) * NZP, (j1 * RES + i1) * NZP);
+      wts[l] = make_float2(__fsub_rn(xb, fx), __fsub_rn(yb, fy));
     }
     __syncthreads();
     for (int idx = tid; idx < nl * NZP; idx += nt) {

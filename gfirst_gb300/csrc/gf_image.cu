@@ -93,32 +93,57 @@ __device__ __forceinline__ float zrule(const float* c, int ze, int K, int NZS, c
   return v;
 }
 
-// img_out = img_in * factor, then slice 0 <- slice 1 and slice NZS-1 <-
-// slice NZS-2 (GFIRST.cu:492-496).  Voxel 0's factor (DENOM[0] in the
-// reference) only reaches slice 0, which the edge copy overwrites.
+// img = img * factor, then slice 0 <- slice 1 and slice NZS-1 <- slice
+// NZS-2 (GFIRST.cu:492-496), in place.  One warp owns a column and reads all
+// of its slices before writing any, so the edge slices see the column's old
+// values as the reference's multiply-then-copy order requires.  Voxel 0's
+// factor (DENOM[0] in the reference) only reaches slice 0, which the edge
+// copy overwrites.
+template <int Q>
 __global__ void __launch_bounds__(256) zfilter_update_kernel(const DevGeom g, const float* __restrict__ C,
-                                                             const float* __restrict__ img_in, const Taps5 t5,
-                                                             float* __restrict__ img_out) {
+                                                             const Taps5 t5, float* img) {
   const int lane = threadIdx.x & 31;
   const int colidx = blockIdx.x * 8 + (threadIdx.x >> 5);
-  const int z = blockIdx.y * 32 + lane;
-  if (colidx >= g.res * g.res) return;
+  if (colidx >= g.res * g.res) return;  // whole warp
   const size_t cb = (size_t)colidx * g.nzp;
   const int NZS = g.nzs;
-  if (z >= NZS) {
-    img_out[cb + z] = 0.f;
-    return;
+  float v[Q];
+#pragma unroll
+  for (int q = 0; q < Q; q++) v[q] = img[cb + lane + 32 * q];
+  const float s1 = __shfl_sync(0xffffffffu, v[0], 1);
+  float sl = 0.f;
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const float w = __shfl_sync(0xffffffffu, v[q], (NZS - 2) & 31);
+    if (q == (NZS - 2) >> 5) sl = w;
   }
-  const int ze = (z == 0) ? 1 : (z == NZS - 1 ? NZS - 2 : z);
-  const int K = (colidx == 0) ? ze - 1 : ze;
-  const float f = zrule(C + cb, ze, K, NZS, t5);
-  img_out[cb + z] = __fmul_rn(img_in[cb + ze], f);
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const int z = lane + 32 * q;
+    float out = 0.f;
+    if (z < NZS) {
+      const int ze = (z == 0) ? 1 : (z == NZS - 1 ? NZS - 2 : z);
+      const float iv = (z == 0) ? s1 : (z == NZS - 1 ? sl : v[q]);
+      const int K = (colidx == 0) ? ze - 1 : ze;
+      out = __fmul_rn(iv, zrule(C + cb, ze, K, NZS, t5));
+    }
+    img[cb + z] = out;
+  }
 }
 
-cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const float* img_in, const Taps5& t5,
-                                  float* img_out, cudaStream_t st) {
-  dim3 grid((g.res * g.res + 7) / 8, g.nzp / 32);
-  zfilter_update_kernel<<<grid, 256, 0, st>>>(g, C, img_in, t5, img_out);
+cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const Taps5& t5, float* img, cudaStream_t st) {
+  dim3 grid((g.res * g.res + 7) / 8);
+  switch (g.nzp / 32) {
+    case 1: zfilter_update_kernel<1><<<grid, 256, 0, st>>>(g, C, t5, img); break;
+    case 2: zfilter_update_kernel<2><<<grid, 256, 0, st>>>(g, C, t5, img); break;
+    case 3: zfilter_update_kernel<3><<<grid, 256, 0, st>>>(g, C, t5, img); break;
+    case 4: zfilter_update_kernel<4><<<grid, 256, 0, st>>>(g, C, t5, img); break;
+    case 5: zfilter_update_kernel<5><<<grid, 256, 0, st>>>(g, C, t5, img); break;
+    case 6: zfilter_update_kernel<6><<<grid, 256, 0, st>>>(g, C, t5, img); break;
+    case 7: zfilter_update_kernel<7><<<grid, 256, 0, st>>>(g, C, t5, img); break;
+    case 8: zfilter_update_kernel<8><<<grid, 256, 0, st>>>(g, C, t5, img); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

@@ -63,6 +63,7 @@ struct gf_ctx {
   float gtab_sigma = -1.f;
   // scratch of the operator entry points, allocated on first use
   int64_t launches = 0;  // kernels launched by this context
+  int bp_warps = 8;      // back-projector warps (columns) per block
   float* s_img = nullptr;
   float* s_img2 = nullptr;
   float* s_numer = nullptr;
@@ -84,8 +85,7 @@ struct gf_recon {
   int ntypes = 1;
   bool loaded = false;
   std::vector<gf::DevBuf> owned;
-  float* img[2] = {nullptr, nullptr};  // z-fast images (doubles, triples)
-  float* img_alt = nullptr;            // update output, swapped with img[t]
+  float* img[2] = {nullptr, nullptr};  // z-fast images (doubles, triples), updated in place
   float* psf = nullptr;
   float* numer = nullptr;
   float* denom = nullptr;
@@ -107,6 +107,7 @@ struct gf_recon {
   int iters_done = 0;
   int64_t subs_done = 0;
   int cur_type = 0, cur_sub = 0;
+  int64_t launches_per_iteration = 0;  // kernels in one captured iteration
 
   // stage profiling
   struct StageEv {

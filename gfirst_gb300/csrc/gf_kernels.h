@@ -32,15 +32,14 @@ struct BpArgs {
   float* numer;            // z-fast
   float* denom;            // z-fast
 };
-cudaError_t launch_bp(const BpArgs& a, cudaStream_t st);
+cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st);
 
 // ---- image kernels (gf_image.cu) ----
 // out = XY PSF of `in`; with `den` the input is the update ratio in/den.
 cudaError_t launch_conv_xy(const DevGeom& g, const float* in, const float* den, const Taps9& t, float* out,
                            cudaStream_t st);
-// img_out = img_in * axial_filter(C) with the edge-slice copy.
-cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const float* img_in, const Taps5& t5,
-                                  float* img_out, cudaStream_t st);
+// img *= axial_filter(C), then the edge-slice copy; in place.
+cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const Taps5& t5, float* img, cudaStream_t st);
 // Axial filter alone, z-fast in/out (voxel 0 keeps out's value).
 cudaError_t launch_zfilter(const DevGeom& g, const float* C, const Taps5& t5, float* out, cudaStream_t st);
 cudaError_t launch_file_to_zfast(const DevGeom& g, const float* in, float* out, cudaStream_t st);

@@ -85,6 +85,7 @@ size_t FpSchedule::smem_bytes() const {
 }
 
 bool make_fp_schedule(const Plan& p, int R, int lc, FpSchedule* out) {
+  if (lc < 1 || lc > 256 || R < 1) return false;
   FpSchedule f;
   f.R = R;
   f.lc = lc;

@@ -106,15 +106,12 @@ gf_status gf_recon::subiteration(int t, int s) {
   }
   BpArgs b{c->dg, s, na, corrcal, numer, denom};
   stage_begin(GF_STAGE_BP);
-  GF_LAUNCH(c, launch_bp(b, st));
+  GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
   stage_end();
   stage_begin(GF_STAGE_UPDATE);
   GF_LAUNCH(c, launch_conv_xy(c->dg, numer, denom, g_bw, ctmp, st));
-  GF_LAUNCH(c, launch_zfilter_update(c->dg, ctmp, img[t], g5, img_alt, st));
+  GF_LAUNCH(c, launch_zfilter_update(c->dg, ctmp, g5, img[t], st));
   stage_end();
-  float* tmp = img[t];
-  img[t] = img_alt;
-  img_alt = tmp;
   if (t == 1 && s == pl.nsub - 1) {
     // GFIRST.cu:512-524: r=4, sigma3D=0.75, sigmaI=0.025, max_ref over the doubles image
     stage_begin(GF_STAGE_BILATERAL);
@@ -163,7 +160,6 @@ gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out)
   ALLOC(r->proj_ref, pl.ndata);
   if (prm->mode >= 1) {
     ALLOC(r->img[1], pl.nvoxp);
-    ALLOC(r->img_alt, pl.nvoxp);
     ALLOC(r->psf, pl.nvoxp);
     ALLOC(r->numer, pl.nvoxp);
     ALLOC(r->denom, pl.nvoxp);

@@ -208,6 +208,29 @@ gf_status gf_recon_get_proj_ref(gf_recon* r, float* h_out);
 /* SINOG_VLOR.raw contents of the last triples sub-iteration (GFIRST.cu:391-394). */
 gf_status gf_recon_get_sinog_vlor(gf_recon* r, float* h_out);
 
+/* ---- batches of frames (no counterpart in the reference, which
+ * reconstructs one acquisition per run) ------------------------------------ */
+typedef struct gf_batch gf_batch;
+/* Groups loaded reconstructions (frames) that advance together; frames may
+ * have different subset counts and modes, each keeps its own resident data.
+ * The recons must outlive the batch. */
+gf_status gf_batch_create(int32_t nframes, gf_recon* const* frames, gf_batch** out);
+void gf_batch_destroy(gf_batch* b);
+/* Advances every frame by n full iterations.  With use_graph != 0 one
+ * iteration of all frames is captured once into a CUDA graph -- each frame's
+ * kernels on its own branch, so frames overlap on the device -- and replayed
+ * n times; frames must stand at an iteration boundary.  With use_graph = 0
+ * the kernels are launched directly, frame by frame.  Asynchronous. */
+gf_status gf_batch_iterate(gf_batch* b, int32_t n, int32_t use_graph);
+gf_status gf_batch_synchronize(gf_batch* b);
+
+/* ---- autotuning (no counterpart in the reference) ------------------------ */
+/* Times the forward projector's thread schedules (run length R of planes per
+ * thread, samples per shared-memory chunk) and the back projector's warps per
+ * block on this context's geometry with synthetic data, keeps the fastest,
+ * and reports them.  Subsequent launches of the context use them. */
+gf_status gf_tune(gf_ctx* ctx, int32_t* fp_run, int32_t* fp_chunk, int32_t* bp_warps);
+
 /* ---- measurement (no counterpart in the reference, which only prints a
  * one-second wall clock, GFIRST.cu:51-52, 572-573) ------------------------- */
 typedef enum gf_stage {
