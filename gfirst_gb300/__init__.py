@@ -36,7 +36,11 @@ class _CGeom(ctypes.Structure):
 
 class _CParams(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("niter", ctypes.c_int32), ("psf_fw", ctypes.c_float),
-                ("psf_bw", ctypes.c_float), ("scale_d", ctypes.c_float), ("scale_t", ctypes.c_float)]
+                ("psf_bw", ctypes.c_float), ("scale_d", ctypes.c_float), ("scale_t", ctypes.c_float),
+                ("storage", ctypes.c_int32)]
+
+
+STORE = {"f32": 0, "f16": 1, "bf16": 2}
 
 
 @dataclass(frozen=True)
@@ -250,10 +254,11 @@ def recon_defaults(mode: int) -> _CParams:
 class Recon:
     """gf_recon: one reconstruction of a CLI mode, resident on the device."""
 
-    def __init__(self, ctx: Context, mode: int, niter: int = 60, psf_fw: float = 1.5, psf_bw: float = 1.5):
+    def __init__(self, ctx: Context, mode: int, niter: int = 60, psf_fw: float = 1.5, psf_bw: float = 1.5,
+                 storage: str = "f32"):
         self.ctx, self.mode = ctx, mode
         p = recon_defaults(mode)
-        p.niter, p.psf_fw, p.psf_bw = niter, psf_fw, psf_bw
+        p.niter, p.psf_fw, p.psf_bw, p.storage = niter, psf_fw, psf_bw, STORE[storage]
         self.params = p
         h = ctypes.c_void_p()
         _ck(lib().gf_recon_create(ctx.h, ctypes.byref(p), ctypes.byref(h)))

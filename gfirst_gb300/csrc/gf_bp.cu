@@ -28,8 +28,10 @@ __device__ __forceinline__ float2 lerp2(float2 a, float2 b, float2 w) {
   return __ffma2_rn(w, __fadd2_rn(b, make_float2(-a.x, -a.y)), a);
 }
 
-template <int Q>
+template <int Q, int STORE>
 __global__ void __launch_bounds__(256) bp_kernel(const BpArgs a, int rmax) {
+  using Pair = typename PairT<STORE>::type;
+  const Pair* cc = static_cast<const Pair*>(a.corrcal);
   extern __shared__ __align__(16) unsigned char smraw[];
   const DevGeom& g = a.g;
   const int nwarps = blockDim.x >> 5;
@@ -73,15 +75,15 @@ __global__ void __launch_bounds__(256) bp_kernel(const BpArgs a, int rmax) {
       const int4 e = my[tl];
       const float2 al2 = make_float2(__int_as_float(e.z), __int_as_float(e.z));
       const float t = __fmul_rn(__int_as_float(e.w), sg.fz);  // yrot*fz
-      const float2* p0 = a.corrcal + e.x + sg.blk;
-      const float2* p1 = a.corrcal + e.y + sg.blk;
+      const Pair* p0 = cc + e.x + sg.blk;
+      const Pair* p1 = cc + e.y + sg.blk;
       float2 c0[Q + 1], c1[Q + 1];
 #pragma unroll
       for (int k = 0; k <= Q; k++) {
         const int r = lane + 32 * k;
         if (r < nrow) {
-          c0[k] = __ldg(p0 + r);
-          c1[k] = __ldg(p1 + r);
+          c0[k] = pair_f(__ldg(p0 + r));
+          c1[k] = pair_f(__ldg(p1 + r));
         }
       }
       __syncwarp();
@@ -125,15 +127,16 @@ cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st) {
   size_t smem = (size_t)warps * (a.na * sizeof(int4) + rmax * sizeof(float2));
   dim3 grid((a.g.res * a.g.res + warps - 1) / warps);
   void (*k)(BpArgs, int) = nullptr;
-  switch (Q) {
-    case 1: k = bp_kernel<1>; break;
-    case 2: k = bp_kernel<2>; break;
-    case 3: k = bp_kernel<3>; break;
-    case 4: k = bp_kernel<4>; break;
-    case 5: k = bp_kernel<5>; break;
-    case 6: k = bp_kernel<6>; break;
-    case 7: k = bp_kernel<7>; break;
-    case 8: k = bp_kernel<8>; break;
+  switch (a.storage * 16 + Q) {
+#define GF_BP_CASE(S, QQ) \
+  case S * 16 + QQ: k = bp_kernel<QQ, S>; break;
+    GF_BP_CASE(0, 1) GF_BP_CASE(0, 2) GF_BP_CASE(0, 3) GF_BP_CASE(0, 4)
+    GF_BP_CASE(0, 5) GF_BP_CASE(0, 6) GF_BP_CASE(0, 7) GF_BP_CASE(0, 8)
+    GF_BP_CASE(1, 1) GF_BP_CASE(1, 2) GF_BP_CASE(1, 3) GF_BP_CASE(1, 4)
+    GF_BP_CASE(1, 5) GF_BP_CASE(1, 6) GF_BP_CASE(1, 7) GF_BP_CASE(1, 8)
+    GF_BP_CASE(2, 1) GF_BP_CASE(2, 2) GF_BP_CASE(2, 3) GF_BP_CASE(2, 4)
+    GF_BP_CASE(2, 5) GF_BP_CASE(2, 6) GF_BP_CASE(2, 7) GF_BP_CASE(2, 8)
+#undef GF_BP_CASE
     default: return cudaErrorInvalidValue;
   }
   if (smem > 48 * 1024) {

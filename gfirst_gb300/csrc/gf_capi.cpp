@@ -410,7 +410,7 @@ gf_status gf_back_project(gf_ctx* c, const float* d_corr, const float* d_calib, 
   GF_TRY(c->ensure_scratch());
   const int na = c->plan.sub_nang[subset];
   GF_LAUNCH(c, launch_corrcal_from_file(c->dg, c->d_rowmap, subset, na, d_corr, d_calib, c->s_cc, c->stream));
-  BpArgs b{c->dg, subset, na, c->s_cc, c->s_numer, c->s_denom};
+  BpArgs b{c->dg, subset, na, c->s_cc, c->s_numer, c->s_denom, 0};
   GF_LAUNCH(c, launch_bp(b, c->bp_warps, c->stream));
   GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_numer, 1.f, 0, d_numer, c->stream));
   GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_denom, 1.f, 0, d_denom, c->stream));

@@ -6,6 +6,8 @@
 // source writes as two operations.  Interpolation is lerp(a,b,w) =
 // fma(w, b-a, a), the rule the CPU oracle uses for the texture unit.
 #pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -28,6 +30,14 @@ struct DevGeom {
 };
 
 #ifdef __CUDACC__
+__device__ __forceinline__ float2 pair_f(float2 v) { return v; }
+__device__ __forceinline__ float2 pair_f(__half2 v) { return __half22float2(v); }
+__device__ __forceinline__ float2 pair_f(__nv_bfloat162 v) { return __bfloat1622float2(v); }
+template <class P> __device__ __forceinline__ P pair_from(float2 v);
+template <> __device__ __forceinline__ float2 pair_from<float2>(float2 v) { return v; }
+template <> __device__ __forceinline__ __half2 pair_from<__half2>(float2 v) { return __float22half2_rn(v); }
+template <> __device__ __forceinline__ __nv_bfloat162 pair_from<__nv_bfloat162>(float2 v) { return __float22bfloat162_rn(v); }
+
 __device__ __forceinline__ float lerp_rn(float a, float b, float w) { return __fmaf_rn(w, __fsub_rn(b, a), a); }
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
 

@@ -23,8 +23,9 @@
 
 namespace gf {
 
-template <int R, bool RATIO, bool FULL>
+template <int R, bool RATIO, bool FULL, int STORE>
 __global__ void __launch_bounds__(512) fp_kernel(const FpArgs a) {
+  using Pair = typename PairT<STORE>::type;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int lc = a.lc, cw = a.cw;
   int4* offs = reinterpret_cast<int4*>(smraw);              // [lc]
@@ -128,18 +129,19 @@ __global__ void __launch_bounds__(512) fp_kernel(const FpArgs a) {
         const float2 db = a.dbg[o];
         const float s = __fadd_rn(proj, db.y);
         const float corr = (s >= 0.01f) ? __fdiv_rn(db.x, s) : -1000.f;
-        const float2 cc = make_float2(corr, a.cal[o]);
-        a.corrcal[o] = cc;
-        if (j == 0 && (run.w & 1)) a.corrcal[o - 1] = (run.x == 0) ? cc : sentinel;
-        if (j == run.z - 1 && (run.w & 2)) a.corrcal[o + 1] = (run.x == 0) ? cc : sentinel;
+        Pair* cc_out = static_cast<Pair*>(a.corrcal);
+        const Pair cc = pair_from<Pair>(make_float2(corr, a.cal[o]));
+        cc_out[o] = cc;
+        if (j == 0 && (run.w & 1)) cc_out[o - 1] = (run.x == 0) ? cc : pair_from<Pair>(sentinel);
+        if (j == run.z - 1 && (run.w & 2)) cc_out[o + 1] = (run.x == 0) ? cc : pair_from<Pair>(sentinel);
       }
     }
   }
 }
 
-template <int R, bool RATIO, bool FULL>
+template <int R, bool RATIO, bool FULL, int STORE>
 static cudaError_t launch_fp_t(const FpArgs& a, const FpSchedule& s, cudaStream_t st) {
-  auto k = fp_kernel<R, RATIO, FULL>;
+  auto k = fp_kernel<R, RATIO, FULL, STORE>;
   size_t smem = s.smem_bytes();
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -151,13 +153,18 @@ static cudaError_t launch_fp_t(const FpArgs& a, const FpSchedule& s, cudaStream_
 
 template <int R>
 static cudaError_t launch_fp_r(const FpArgs& a, const FpSchedule& s, cudaStream_t st) {
-  if (a.corrcal && a.proj_full) return launch_fp_t<R, true, true>(a, s, st);
-  if (a.corrcal) return launch_fp_t<R, true, false>(a, s, st);
-  return launch_fp_t<R, false, true>(a, s, st);
+  if (!a.corrcal) return launch_fp_t<R, false, true, 0>(a, s, st);
+  switch (a.storage) {
+    case 0: return a.proj_full ? launch_fp_t<R, true, true, 0>(a, s, st) : launch_fp_t<R, true, false, 0>(a, s, st);
+    case 1: return launch_fp_t<R, true, false, 1>(a, s, st);
+    case 2: return launch_fp_t<R, true, false, 2>(a, s, st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_fp(const FpArgs& a, const FpSchedule& s, cudaStream_t st) {
   if (!a.corrcal && !a.proj_full) return cudaErrorInvalidValue;
+  if (a.corrcal && a.proj_full && a.storage != 0) return cudaErrorInvalidValue;
   switch (s.R) {
     case 9: return launch_fp_r<9>(a, s, st);
     case 17: return launch_fp_r<17>(a, s, st);

@@ -91,7 +91,7 @@ struct gf_recon {
   float* denom = nullptr;
   float* ctmp = nullptr;
   float* filt = nullptr;
-  float2* corrcal = nullptr;
+  void* corrcal = nullptr;  // (ratio, mask) pairs of the current subset, gf_recon_params::storage
   float2* dbg[2] = {nullptr, nullptr};
   float* cal = nullptr;
   float* proj_ref = nullptr;

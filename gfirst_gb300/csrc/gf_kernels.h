@@ -1,11 +1,19 @@
 // gf_kernels.h -- host-callable launchers of the sm_103a kernels.
 #pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "gf_device.cuh"
 #include "gf_plan.h"
 
 namespace gf {
+
+// (ratio, mask) pair storage of the per-subset sinogram.
+template <int S> struct PairT;
+template <> struct PairT<0> { using type = float2; };
+template <> struct PairT<1> { using type = __half2; };
+template <> struct PairT<2> { using type = __nv_bfloat162; };
 
 struct Taps9 { float c[9]; };
 struct Taps5 { float c[5]; };
@@ -19,8 +27,9 @@ struct FpArgs {
   int nruns, padl, cw, lc;
   const float2* dbg;       // subset layout (data*RES, max(bg*RES,0)); with corrcal
   const float* cal;        // subset layout normalization mask; with corrcal
-  float2* corrcal;         // subset layout (corr, calib) output, or null
+  void* corrcal;           // subset layout (corr, calib) pairs output, or null
   float* proj_full;        // file-layout projection output, or null
+  int storage;             // corrcal pair type: 0 float2, 1 __half2, 2 __nv_bfloat162
 };
 cudaError_t launch_fp(const FpArgs& a, const FpSchedule& s, cudaStream_t st);
 
@@ -28,9 +37,10 @@ cudaError_t launch_fp(const FpArgs& a, const FpSchedule& s, cudaStream_t st);
 struct BpArgs {
   DevGeom g;
   int subset, na;          // na: angles in this subset
-  const float2* corrcal;   // subset layout (corr, calib)
+  const void* corrcal;     // subset layout (corr, calib) pairs
   float* numer;            // z-fast
   float* denom;            // z-fast
+  int storage;             // corrcal pair type, as FpArgs::storage
 };
 cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st);
 
@@ -60,8 +70,8 @@ cudaError_t launch_build_cal(const DevGeom& g, const int2* rowmap, const float* 
 cudaError_t launch_corrcal_from_file(const DevGeom& g, const int2* rowmap, int subset, int na, const float* corr,
                                      const float* calib, float2* corrcal, cudaStream_t st);
 cudaError_t launch_ratio_gather(const DevGeom& g, const int2* rowmap, int subset, int na, const float* proj_full,
-                                const float* datos_v, const float2* dbg_t, const float* cal, float2* corrcal,
-                                cudaStream_t st);
+                                const float* datos_v, const float2* dbg_t, const float* cal, void* corrcal,
+                                int storage, cudaStream_t st);
 cudaError_t launch_ratio_file(const DevGeom& g, int subset, const float* proj, const float* data, const float* bg,
                               float* corr, cudaStream_t st);
 cudaError_t launch_norm_mask(const DevGeom& g, const float* proj_blank, const float* blank, float* calib,

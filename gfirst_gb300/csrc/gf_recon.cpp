@@ -94,17 +94,19 @@ gf_status gf_recon::subiteration(int t, int s) {
     stage_begin(GF_STAGE_VLOR);
     GF_CK(cudaMemsetAsync(datos_v, 0, (size_t)pl.ndata * sizeof(float), st));
     GF_LAUNCH(c, launch_vlor_split(c->dg, events, nev, proj_t, blankt, datos_v, st));
-    GF_LAUNCH(c, launch_ratio_gather(c->dg, c->d_rowmap, s, na, proj_t, datos_v, dbg[1] + off, cal + off, corrcal, st));
+    GF_LAUNCH(c, launch_ratio_gather(c->dg, c->d_rowmap, s, na, proj_t, datos_v, dbg[1] + off, cal + off, corrcal,
+                                     p.storage, st));
     stage_end();
   } else {
     a.dbg = dbg[t] + off;
     a.cal = cal + off;
     a.corrcal = corrcal;
+    a.storage = p.storage;
     stage_begin(GF_STAGE_FP);
     GF_LAUNCH(c, launch_fp(a, c->fps, st));
     stage_end();
   }
-  BpArgs b{c->dg, s, na, corrcal, numer, denom};
+  BpArgs b{c->dg, s, na, corrcal, numer, denom, p.storage};
   stage_begin(GF_STAGE_BP);
   GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
   stage_end();
@@ -135,6 +137,7 @@ gf_status gf_recon_defaults(int32_t mode, gf_recon_params* out) {
   out->psf_bw = 1.5f;
   out->scale_d = (float)(3.70e-4 * 162.0);
   out->scale_t = (float)(3.70e-4 * 162.0);
+  out->storage = GF_STORE_F32;
   return GF_OK;
 }
 
@@ -143,6 +146,7 @@ gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out)
   *out = nullptr;
   if (prm->mode < 0 || prm->mode > 3) return set_error(GF_ERR_ARG, "mode must be 0..3");
   if (prm->niter < 0) return set_error(GF_ERR_ARG, "niter must be >= 0");
+  if (prm->storage < GF_STORE_F32 || prm->storage > GF_STORE_BF16) return set_error(GF_ERR_ARG, "unknown storage");
   GF_CK(cudaSetDevice(c->device));
   gf_recon* r = new gf_recon();
   r->ctx = c;
@@ -164,7 +168,8 @@ gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out)
     ALLOC(r->numer, pl.nvoxp);
     ALLOC(r->denom, pl.nvoxp);
     ALLOC(r->ctmp, pl.nvoxp);
-    ALLOC(r->corrcal, (size_t)pl.amax * pl.g.nrad * pl.PS);
+    if ((st = r->alloc((size_t)pl.amax * pl.g.nrad * pl.PS * (prm->storage == GF_STORE_F32 ? 8 : 4), &r->corrcal)) != GF_OK)
+      return fail(st);
     ALLOC(r->dbg[0], pl.all_elems());
     ALLOC(r->cal, pl.all_elems());
   }

@@ -134,10 +134,11 @@ cudaError_t launch_corrcal_from_file(const DevGeom& g, const int2* rowmap, int s
 
 // Ratio for the VLOR triples (GFIRST.cu:415-430 with val_dato = datos_v*RES,
 // GFIRST.cu:397, 421) written as (corr, calib) pairs of one subset.
+template <class Pair>
 __global__ void ratio_gather_kernel(const DevGeom g, const int2* __restrict__ rowmap, int subset,
                                     const float* __restrict__ proj_full, const float* __restrict__ datos_v,
                                     const float2* __restrict__ dbg_t, const float* __restrict__ cal,
-                                    float2* __restrict__ cc, size_t n) {
+                                    Pair* __restrict__ cc, size_t n) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int p = (int)(i % g.PS);
@@ -155,15 +156,20 @@ __global__ void ratio_gather_kernel(const DevGeom g, const int2* __restrict__ ro
     const float data = __fmul_rn(datos_v[lor], (float)g.res);
     v = make_float2(ratio_rule(proj_full[lor], data, dbg_t[e].y), cal[e]);
   }
-  cc[i] = v;
+  cc[i] = pair_from<Pair>(v);
 }
 
 cudaError_t launch_ratio_gather(const DevGeom& g, const int2* rowmap, int subset, int na, const float* proj_full,
-                                const float* datos_v, const float2* dbg_t, const float* cal, float2* corrcal,
-                                cudaStream_t st) {
+                                const float* datos_v, const float2* dbg_t, const float* cal, void* corrcal,
+                                int storage, cudaStream_t st) {
   const size_t n = (size_t)na * g.nrad * g.PS;
-  ratio_gather_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, rowmap, subset, proj_full, datos_v, dbg_t,
-                                                                    cal, corrcal, n);
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  switch (storage) {
+    case 0: ratio_gather_kernel<<<nb, 256, 0, st>>>(g, rowmap, subset, proj_full, datos_v, dbg_t, cal, static_cast<float2*>(corrcal), n); break;
+    case 1: ratio_gather_kernel<<<nb, 256, 0, st>>>(g, rowmap, subset, proj_full, datos_v, dbg_t, cal, static_cast<__half2*>(corrcal), n); break;
+    case 2: ratio_gather_kernel<<<nb, 256, 0, st>>>(g, rowmap, subset, proj_full, datos_v, dbg_t, cal, static_cast<__nv_bfloat162*>(corrcal), n); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

@@ -106,7 +106,7 @@ extern "C" gf_status gf_tune(gf_ctx* c, int32_t* fp_run, int32_t* fp_chunk, int3
   int best_w = c->bp_warps;
   float best_bp = 3.0e38f;
   for (int w : {4, 8}) {
-    BpArgs b{c->dg, 0, p.sub_nang[0], c->s_cc, c->s_numer, c->s_denom};
+    BpArgs b{c->dg, 0, p.sub_nang[0], c->s_cc, c->s_numer, c->s_denom, 0};
     float ms = 0.f;
     s = time_it([&] { return launch_bp(b, w, st); }, &ms);
     if (s != GF_OK) return done(s);

@@ -1,6 +1,7 @@
 """Kernel micro-benchmark: time one projector stage on a named geometry.
 
     python -m gfirst_gb300.kbench --op bp|fp|subiter [--geometry preclinical] [--subsets 16] [--reps 5]
+                                  [--storage f32|f16|bf16] [--tune]
 
 Runs a mode-1 reconstruction's stages on synthetic data and reports the
 device time per launch from the library's own stage events.  Small enough to
@@ -18,20 +19,21 @@ import gfirst_gb300 as gf
 GEOMS = {"preclinical": gf.Geometry.preclinical, "reference": gf.Geometry.reference, "small": gf.Geometry.small}
 
 
-def run(op: str, geometry: str, nsub: int, reps: int, fp_r: int = 0) -> dict:
+def run(op: str, geometry: str, nsub: int, reps: int, storage: str = "f32", tune: bool = False) -> dict:
     g = GEOMS[geometry]()
     ctx = gf.Context(g, nsub=nsub)
+    tuned = ctx.tune() if tune else None
     P, ndata, nvox = gf.sizes(g)
     rs = np.random.RandomState(5)
     dsino = np.concatenate([rs.poisson(20.0, ndata), np.zeros(ndata)]).astype(np.float32)
     norm = rs.uniform(0.85, 1.15, ndata).astype(np.float32)
-    r = gf.Recon(ctx, 1, niter=1)
+    r = gf.Recon(ctx, 1, niter=1, storage=storage)
     r.load(dsino=dsino, norm=norm)
     r.subiteration()  # warm-up
     r.profile(True)
     for _ in range(reps):
         r.subiteration()
-    out = {"geometry": geometry, "subsets": nsub, "reps": reps}
+    out = {"geometry": geometry, "subsets": nsub, "reps": reps, "storage": storage, "tuned": tuned}
     for name, sid in gf.STAGES.items():
         tot, n = r.profile_read(sid)
         if n:
@@ -47,8 +49,10 @@ def main() -> None:
     ap.add_argument("--geometry", default="preclinical", choices=sorted(GEOMS))
     ap.add_argument("--subsets", type=int, default=16)
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
+    ap.add_argument("--tune", action="store_true")
     a = ap.parse_args()
-    print(json.dumps(run(a.op, a.geometry, a.subsets, a.reps)))
+    print(json.dumps(run(a.op, a.geometry, a.subsets, a.reps, a.storage, a.tune)))
 
 
 if __name__ == "__main__":

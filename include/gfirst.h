@@ -177,7 +177,12 @@ typedef struct gf_recon_params {
   float psf_bw;    /* PSF_BW, GFIRST.h:27 */
   float scale_d;   /* scale_D, GFIRST.h:29 */
   float scale_t;   /* scale_T, GFIRST.h:30 */
+  int32_t storage; /* per-subset (ratio, mask) sinogram storage: GF_STORE_F32
+                      (the reference's precision), GF_STORE_F16 or
+                      GF_STORE_BF16; arithmetic stays FP32 */
 } gf_recon_params;
+
+enum { GF_STORE_F32 = 0, GF_STORE_F16 = 1, GF_STORE_BF16 = 2 };
 
 /* Reference defaults (GFIRST.h:21-30). */
 gf_status gf_recon_defaults(int32_t mode, gf_recon_params* out);

@@ -417,3 +417,25 @@ def test_tune_keeps_results(gf):
     ctx.back_project(ctx.put(corr), ctx.put(calib), 2, n, dd)
     wn, wd = o.bp(corr, calib, 4, 2)
     assert np.array_equal(n.download(), wn) and np.array_equal(dd.download(), wd)
+
+
+# ---------------------------------------------------------------- reduced-precision storage
+@pytest.mark.parametrize("storage,tol", [("f16", IMG_TOL), ("bf16", 1e-2)])
+def test_reduced_precision_ratio_storage(gf, storage, tol):
+    """(ratio, mask) sinogram pairs stored in 16 bits, arithmetic in FP32: the
+    image error against the FP64 oracle stays within `tol` (FP16: the 1e-3
+    image bound; BF16 keeps 8 mantissa bits and is reported at 1e-2)."""
+    geo = case("tinyb")
+    d = parsed("tinyb")
+    o64 = gfo.Oracle(geo, "f64")
+    exact = o64.recon(1, nsub=2, niter=5, dsino=d["dsino"], norm=d["norm"])["img_d"]
+    ctx = gf.Context(gf.Geometry(*geo), nsub=2)
+    r = gf.Recon(ctx, 1, niter=5, storage=storage)
+    r.load(dsino=d["dsino"], norm=d["norm"])
+    r.iterate(5)
+    err = rel(r.image(0), exact)
+    ref = gf.Recon(ctx, 1, niter=5)
+    ref.load(dsino=d["dsino"], norm=d["norm"])
+    ref.iterate(5)
+    assert err < tol, err
+    assert rel(ref.image(0), exact) < IMG_TOL
