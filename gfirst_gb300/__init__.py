@@ -88,6 +88,7 @@ def _load() -> ctypes.CDLL:
     lib.gf_destroy.restype = None
     lib.gf_recon_destroy.restype = None
     lib.gf_batch_destroy.restype = None
+    lib.gf_server_destroy.restype = None
     lib.gf_copy_to_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
     lib.gf_copy_to_host.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
     lib.gf_device_alloc.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
@@ -340,6 +341,80 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class _CRequest(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("geometry", _CGeom), ("nsubsets", ctypes.c_int32),
+                ("niter", ctypes.c_int32), ("storage", ctypes.c_int32), ("h_image", ctypes.c_void_p),
+                ("h_dsino", ctypes.c_void_p), ("h_norm", ctypes.c_void_p), ("h_out", ctypes.c_void_p)]
+
+
+class _CServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in ("submitted", "completed", "failed", "queued", "active")] + \
+               [(n, ctypes.c_double) for n in ("p50_ms", "p99_ms", "mean_ms", "max_ms", "throughput_per_s")] + \
+               [(n, ctypes.c_int64) for n in ("bytes_in_use", "peak_bytes", "budget_bytes")] + \
+               [("peak_active", ctypes.c_int32)]
+
+
+class Server:
+    """gf_server: HBM-budget admission and continuous batching on one device."""
+
+    def __init__(self, budget_bytes: int, max_active: int = 8, device: int = 0):
+        h = ctypes.c_void_p()
+        _ck(lib().gf_server_create(device, ctypes.c_int64(int(budget_bytes)), max_active, ctypes.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    def submit_recon(self, g: Geometry, dsino, norm, nsub: int = 1, niter: int = 2, storage: str = "f32"):
+        P, ndata, nvox = sizes(g)
+        dsino = np.ascontiguousarray(dsino, np.float32)
+        norm = np.ascontiguousarray(norm, np.float32)
+        out = np.empty(nvox, np.float32)
+        q = _CRequest(0, g.c(), nsub, niter, STORE[storage], None, _ptr(dsino), _ptr(norm), _ptr(out))
+        rid = ctypes.c_int64()
+        _ck(lib().gf_server_submit(self.h, ctypes.byref(q), ctypes.byref(rid)))
+        self._keep[rid.value] = (dsino, norm, out)
+        return rid.value
+
+    def submit_project(self, g: Geometry, image, nsub: int = 1):
+        P, ndata, nvox = sizes(g)
+        image = np.ascontiguousarray(image, np.float32)
+        out = np.empty(ndata, np.float32)
+        q = _CRequest(1, g.c(), nsub, 0, 0, _ptr(image), None, None, _ptr(out))
+        rid = ctypes.c_int64()
+        _ck(lib().gf_server_submit(self.h, ctypes.byref(q), ctypes.byref(rid)))
+        self._keep[rid.value] = (image, out)
+        return rid.value
+
+    def wait(self, rid: int):
+        lat = ctypes.c_double()
+        _ck(lib().gf_server_wait(self.h, ctypes.c_int64(rid), ctypes.byref(lat)))
+        keep = self._keep.pop(rid)
+        return keep[-1], lat.value
+
+    def stats(self) -> dict:
+        s = _CServerStats()
+        _ck(lib().gf_server_get_stats(self.h, ctypes.byref(s)))
+        return {n: getattr(s, n) for n, _ in _CServerStats._fields_}
+
+    def close(self) -> None:
+        if self.h:
+            lib().gf_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def recon_bytes(g: Geometry, nsub: int, mode: int = 1, storage: str = "f32") -> int:
+    p = recon_defaults(mode)
+    p.storage = STORE[storage]
+    b = ctypes.c_int64()
+    _ck(lib().gf_recon_bytes(ctypes.byref(g.c()), nsub, ctypes.byref(p), ctypes.c_int64(0), ctypes.byref(b)))
+    return b.value
 
 
 def read_sinogram(path, ndata: int):

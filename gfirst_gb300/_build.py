@@ -20,7 +20,7 @@ CUDA = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU = ["gf_fp.cu", "gf_bp.cu", "gf_image.cu", "gf_sino.cu", "gf_noalloc.cu"]
-CPP = ["gf_plan.cpp", "gf_capi.cpp", "gf_recon.cpp", "gf_io.cpp", "gf_batch.cpp", "gf_tune.cpp"]
+CPP = ["gf_plan.cpp", "gf_capi.cpp", "gf_recon.cpp", "gf_io.cpp", "gf_batch.cpp", "gf_tune.cpp", "gf_server.cpp"]
 LIB = OUT / "libgfirst.so"
 CLI = OUT / "gfirst"
 

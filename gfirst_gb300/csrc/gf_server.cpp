@@ -1,0 +1,319 @@
+// gf_server.cpp -- a request loop with HBM-budget admission and continuous
+// batching on one device.
+//
+// Requests (reconstructions and bare projections, of any geometry) wait in
+// arrival order.  A worker thread admits the head of the queue when its
+// device bytes (gf_recon_bytes) fit the remaining budget and fewer than
+// max_active requests run, builds its context (own stream) and
+// reconstruction, and loads its data.  Every active reconstruction keeps one
+// iteration in flight: when its completion event fires the next iteration is
+// queued, so requests of different sizes advance independently and their
+// kernels overlap on the device.  A finished request's image is read back,
+// its memory released, and the queue re-examined.  Results do not depend on
+// what else runs: each request owns its buffers and the kernels are
+// deterministic for modes 0 and 1.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "gf_internal.h"
+
+using namespace gf;
+
+namespace {
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Job {
+  int64_t id = 0;
+  gf_request req{};
+  int64_t bytes = 0;
+  double t_submit = 0, t_done = 0;
+  gf_ctx* ctx = nullptr;
+  gf_recon* rec = nullptr;
+  cudaEvent_t ev = nullptr;
+  bool in_flight = false;
+  int iters = 0;
+  int state = 0;  // 0 queued, 1 active, 2 done
+  gf_status status = GF_OK;
+  std::string err;
+};
+
+}  // namespace
+
+struct gf_server {
+  int device = 0;
+  int64_t budget = 0;
+  int max_active = 1;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Job*> queue;
+  std::vector<Job*> active;
+  std::unordered_map<int64_t, Job*> jobs;
+  int64_t next_id = 1, bytes_in_use = 0, peak_bytes = 0, submitted = 0, completed = 0, failed = 0;
+  int peak_active = 0;
+  double t_first = -1;
+  std::vector<double> lat;
+  bool stop = false;
+  std::thread worker;
+
+  void run();
+  void finish(Job* j, gf_status st);
+  gf_status start(Job* j);
+};
+
+static void release(Job* j) {
+  if (j->ev) cudaEventDestroy(j->ev);
+  if (j->rec) gf_recon_destroy(j->rec);
+  if (j->ctx) gf_destroy(j->ctx);
+  j->ev = nullptr;
+  j->rec = nullptr;
+  j->ctx = nullptr;
+}
+
+void gf_server::finish(Job* j, gf_status st) {
+  release(j);
+  std::lock_guard<std::mutex> lk(mu);
+  j->status = st;
+  if (st != GF_OK) j->err = gf_last_error();
+  j->t_done = now_ms();
+  j->state = 2;
+  bytes_in_use -= j->bytes;
+  if (st == GF_OK) {
+    completed++;
+    lat.push_back(j->t_done - j->t_submit);
+  } else {
+    failed++;
+  }
+  active.erase(std::remove(active.begin(), active.end(), j), active.end());
+  cv_done.notify_all();
+}
+
+gf_status gf_server::start(Job* j) {
+  const gf_request& q = j->req;
+  GF_TRY(gf_create(&q.geometry, q.nsubsets, device, &j->ctx));
+  gf_recon_params p;
+  gf_recon_defaults(q.kind == GF_REQ_PROJECT ? 0 : 1, &p);
+  p.niter = q.niter;
+  p.storage = q.storage;
+  GF_TRY(gf_recon_create(j->ctx, &p, &j->rec));
+  GF_TRY(gf_recon_load(j->rec, q.h_image, q.h_dsino, nullptr, q.h_norm, nullptr, 0));
+  GF_CK(cudaEventCreateWithFlags(&j->ev, cudaEventDisableTiming));
+  return GF_OK;
+}
+
+void gf_server::run() {
+  cudaSetDevice(device);
+  for (;;) {
+    // admission
+    std::vector<Job*> admit;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      if (queue.empty() && active.empty()) {
+        if (stop) return;
+        cv_work.wait(lk, [&] { return stop || !queue.empty(); });
+        if (queue.empty() && stop) return;
+      }
+      while (!queue.empty() && (int)active.size() + (int)admit.size() < max_active) {
+        Job* j = queue.front();
+        if (j->bytes > budget) {  // can never fit
+          queue.pop_front();
+          j->state = 2;
+          j->status = GF_ERR_NOMEM;
+          j->err = "request needs more device memory than the server's budget";
+          j->t_done = now_ms();
+          failed++;
+          cv_done.notify_all();
+          continue;
+        }
+        if (bytes_in_use + j->bytes > budget) break;  // wait for memory, keep arrival order
+        queue.pop_front();
+        bytes_in_use += j->bytes;
+        peak_bytes = std::max(peak_bytes, bytes_in_use);
+        j->state = 1;
+        admit.push_back(j);
+      }
+      for (Job* j : admit) active.push_back(j);
+      peak_active = std::max(peak_active, (int)active.size());
+    }
+    for (Job* j : admit) {
+      gf_status st = start(j);
+      if (st != GF_OK) {
+        finish(j, st);
+        continue;
+      }
+      if (j->req.kind == GF_REQ_PROJECT) finish(j, gf_recon_get_proj_ref(j->rec, j->req.h_out));
+    }
+    // progress: one iteration in flight per active reconstruction
+    std::vector<Job*> act;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      act = active;
+    }
+    bool progressed = !admit.empty();
+    for (Job* j : act) {
+      if (j->in_flight) {
+        cudaError_t e = cudaEventQuery(j->ev);
+        if (e == cudaErrorNotReady) continue;
+        j->in_flight = false;
+        progressed = true;
+        if (e != cudaSuccess) {
+          finish(j, cuda_error(e, "request iteration"));
+          continue;
+        }
+        j->iters++;
+      }
+      if (j->iters >= j->req.niter) {
+        finish(j, gf_recon_get_image(j->rec, 0, 0, j->req.h_out));
+        progressed = true;
+        continue;
+      }
+      gf_status st = gf_recon_iterate(j->rec, 1);
+      if (st == GF_OK && cudaEventRecord(j->ev, j->ctx->stream) != cudaSuccess) st = cuda_error(cudaGetLastError(), "event");
+      if (st != GF_OK) {
+        finish(j, st);
+        continue;
+      }
+      j->in_flight = true;
+      progressed = true;
+    }
+    if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+extern "C" {
+
+gf_status gf_recon_bytes(const gf_geometry* gg, int32_t nsub, const gf_recon_params* p, int64_t nev, int64_t* bytes) {
+  if (!gg || !p || !bytes) return set_error(GF_ERR_ARG, "null argument");
+  Geom geo{gg->res, gg->nzs, gg->nrad, gg->nang, gg->span, gg->nseg, gg->pitch_mm, gg->diam_det_mm, gg->fov_mm};
+  Plan pl;
+  std::string err;
+  if (!make_plan(geo, nsub, &pl, &err)) return set_error(GF_ERR_GEOMETRY, err);
+  const int64_t v = pl.nvoxp * 4, d = pl.ndata * 4, all = pl.all_elems();
+  int64_t b = v + d + 64 * 1024;  // image, proj_ref, context tables
+  if (p->mode == 0) {
+    b += pl.nvox * 4;  // staging
+  } else {
+    b += 5 * v;                                                                   // second image, psf, numer, denom, ctmp
+    b += (int64_t)pl.amax * pl.g.nrad * pl.PS * (p->storage == GF_STORE_F32 ? 8 : 4);  // ratio sinogram
+    b += all * 8 + all * 4;                                                       // data/background, mask
+    b += 3 * d;                                                                   // staging
+  }
+  if (p->mode >= 2) b += all * 8 + v;
+  if (p->mode == 3) b += 3 * d + nev * 8;
+  *bytes = b;
+  return GF_OK;
+}
+
+gf_status gf_server_create(int32_t device, int64_t budget, int32_t max_active, gf_server** out) {
+  if (!out || budget <= 0 || max_active < 1) return set_error(GF_ERR_ARG, "bad argument");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return set_error(GF_ERR_NODEV, "no such CUDA device");
+  }
+  gf_server* s = new gf_server();
+  s->device = device;
+  s->budget = budget;
+  s->max_active = max_active;
+  s->worker = std::thread([s] { s->run(); });
+  *out = s;
+  return GF_OK;
+}
+
+void gf_server_destroy(gf_server* s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  for (auto& kv : s->jobs) {
+    release(kv.second);
+    delete kv.second;
+  }
+  delete s;
+}
+
+gf_status gf_server_submit(gf_server* s, const gf_request* q, int64_t* id) {
+  if (!s || !q || !id || !q->h_out) return set_error(GF_ERR_ARG, "bad argument");
+  if (q->kind == GF_REQ_RECON && (!q->h_dsino || !q->h_norm || q->niter < 0))
+    return set_error(GF_ERR_ARG, "a reconstruction needs a sinogram, a normalization and niter >= 0");
+  if (q->kind == GF_REQ_PROJECT && !q->h_image) return set_error(GF_ERR_ARG, "a projection needs an image");
+  if (q->kind != GF_REQ_RECON && q->kind != GF_REQ_PROJECT) return set_error(GF_ERR_ARG, "unknown request kind");
+  gf_recon_params p;
+  gf_recon_defaults(q->kind == GF_REQ_PROJECT ? 0 : 1, &p);
+  p.storage = q->storage;
+  Job* j = new Job();
+  j->req = *q;
+  gf_status st = gf_recon_bytes(&q->geometry, q->nsubsets, &p, 0, &j->bytes);
+  if (st != GF_OK) {
+    delete j;
+    return st;
+  }
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    j->id = s->next_id++;
+    j->t_submit = now_ms();
+    if (s->t_first < 0) s->t_first = j->t_submit;
+    s->jobs[j->id] = j;
+    s->queue.push_back(j);
+    s->submitted++;
+    *id = j->id;
+  }
+  s->cv_work.notify_all();
+  return GF_OK;
+}
+
+gf_status gf_server_wait(gf_server* s, int64_t id, double* latency_ms) {
+  if (!s) return set_error(GF_ERR_ARG, "null server");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(id);
+  if (it == s->jobs.end()) return set_error(GF_ERR_ARG, "unknown request id");
+  Job* j = it->second;
+  s->cv_done.wait(lk, [&] { return j->state == 2; });
+  if (latency_ms) *latency_ms = j->t_done - j->t_submit;
+  if (j->status != GF_OK) return set_error(j->status, j->err);
+  return GF_OK;
+}
+
+gf_status gf_server_get_stats(gf_server* s, gf_server_stats* o) {
+  if (!s || !o) return set_error(GF_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  *o = gf_server_stats{};
+  o->submitted = s->submitted;
+  o->completed = s->completed;
+  o->failed = s->failed;
+  o->queued = (int64_t)s->queue.size();
+  o->active = (int64_t)s->active.size();
+  o->bytes_in_use = s->bytes_in_use;
+  o->peak_bytes = s->peak_bytes;
+  o->budget_bytes = s->budget;
+  o->peak_active = s->peak_active;
+  if (!s->lat.empty()) {
+    std::vector<double> l = s->lat;
+    std::sort(l.begin(), l.end());
+    auto pct = [&](double f) { return l[std::min(l.size() - 1, (size_t)(f * (double)(l.size() - 1) + 0.5))]; };
+    o->p50_ms = pct(0.50);
+    o->p99_ms = pct(0.99);
+    o->max_ms = l.back();
+    double sum = 0;
+    for (double x : l) sum += x;
+    o->mean_ms = sum / (double)l.size();
+    double last = 0;
+    for (auto& kv : s->jobs)
+      if (kv.second->state == 2 && kv.second->status == GF_OK) last = std::max(last, kv.second->t_done);
+    if (last > s->t_first) o->throughput_per_s = (double)s->completed / ((last - s->t_first) / 1000.0);
+  }
+  return GF_OK;
+}
+
+}  // extern "C"

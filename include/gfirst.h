@@ -229,6 +229,48 @@ void gf_batch_destroy(gf_batch* b);
 gf_status gf_batch_iterate(gf_batch* b, int32_t n, int32_t use_graph);
 gf_status gf_batch_synchronize(gf_batch* b);
 
+/* ---- serving (no counterpart in the reference) ---------------------------- */
+/* Device bytes a reconstruction of these parameters holds (admission control). */
+gf_status gf_recon_bytes(const gf_geometry* g, int32_t nsubsets, const gf_recon_params* p, int64_t nevents,
+                         int64_t* bytes);
+
+typedef struct gf_server gf_server;
+enum { GF_REQ_RECON = 0, GF_REQ_PROJECT = 1 };
+/* One request.  RECON: a mode-1 reconstruction of h_dsino (2*NDATA) and
+ * h_norm (NDATA), niter iterations, result = the raw doubles image (NVOX) in
+ * h_out.  PROJECT: the projection of h_image (NVOX), result = NDATA floats in
+ * h_out.  Host buffers must stay valid until the request completes. */
+typedef struct gf_request {
+  int32_t kind;
+  gf_geometry geometry;
+  int32_t nsubsets;
+  int32_t niter;
+  int32_t storage;  /* GF_STORE_* */
+  const float* h_image;
+  const float* h_dsino;
+  const float* h_norm;
+  float* h_out;
+} gf_request;
+typedef struct gf_server_stats {
+  int64_t submitted, completed, failed, queued, active;
+  double p50_ms, p99_ms, mean_ms, max_ms;  /* submit-to-result latency of completed requests */
+  double throughput_per_s;                 /* completed requests / seconds since the first submit */
+  int64_t bytes_in_use, peak_bytes, budget_bytes;
+  int32_t peak_active;
+} gf_server_stats;
+/* A request loop on one device: requests are admitted in arrival order while
+ * their device bytes fit the budget and fewer than max_active run; every
+ * active request keeps one iteration in flight on its own stream, so work of
+ * different requests overlaps on the device, and finished requests free
+ * their memory for the queue (continuous batching). */
+gf_status gf_server_create(int32_t device, int64_t budget_bytes, int32_t max_active, gf_server** out);
+/* Stops after the queued and active requests finish. */
+void gf_server_destroy(gf_server* s);
+gf_status gf_server_submit(gf_server* s, const gf_request* req, int64_t* id);
+/* Blocks until request id completes; its status (GF_OK or the failure). */
+gf_status gf_server_wait(gf_server* s, int64_t id, double* latency_ms);
+gf_status gf_server_get_stats(gf_server* s, gf_server_stats* out);
+
 /* ---- autotuning (no counterpart in the reference) ------------------------ */
 /* Times the forward projector's thread schedules (run length R of planes per
  * thread, samples per shared-memory chunk) and the back projector's warps per

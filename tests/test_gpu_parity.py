@@ -439,3 +439,59 @@ def test_reduced_precision_ratio_storage(gf, storage, tol):
     ref.iterate(5)
     assert err < tol, err
     assert rel(ref.image(0), exact) < IMG_TOL
+
+
+# ---------------------------------------------------------------- serving
+def _requests(gf):
+    reqs = []
+    for name, nsub, niter in (("tiny", 1, 2), ("tinyb", 2, 3), ("small", 4, 2), ("tinyb", 3, 2), ("tiny", 2, 3)):
+        d = parsed(name)
+        reqs.append(("recon", gf.Geometry(*case(name)), d["dsino"], d["norm"], nsub, niter))
+    for name in ("small", "tinyb"):
+        reqs.append(("project", gf.Geometry(*case(name)), parsed(name)["image"], None, 1, 0))
+    return reqs
+
+
+def _alone(gf, req):
+    kind, g, a, b, nsub, niter = req
+    ctx = gf.Context(g, nsub=nsub)
+    if kind == "project":
+        r = gf.Recon(ctx, 0)
+        r.load(image=a)
+        return r.proj_ref()
+    r = gf.Recon(ctx, 1, niter=niter)
+    r.load(dsino=a, norm=b)
+    r.iterate(niter)
+    return r.image(0)
+
+
+def test_server_results_same_alone_and_in_mix(gf):
+    reqs = _requests(gf)
+    alone = [_alone(gf, q) for q in reqs]
+    sizes = sorted(gf.recon_bytes(q[1], q[4], 1 if q[0] == "recon" else 0) for q in reqs)
+    budget = sizes[-1] + sizes[-2]  # at most two large requests at once: the rest queue
+    srv = gf.Server(budget, max_active=4)
+    ids = []
+    for q in reqs * 2:  # every request twice, interleaved
+        kind, g, a, b, nsub, niter = q
+        ids.append(srv.submit_recon(g, a, b, nsub, niter) if kind == "recon" else srv.submit_project(g, a, nsub))
+    for k, rid in enumerate(ids):
+        out, lat = srv.wait(rid)
+        assert lat > 0
+        assert np.array_equal(out, alone[k % len(reqs)]), k
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(ids) and st["failed"] == 0
+    assert st["peak_bytes"] <= budget
+    assert st["peak_active"] >= 2  # requests overlapped on the device
+    assert 0 < st["p50_ms"] <= st["p99_ms"]
+
+
+def test_server_rejects_request_beyond_its_budget(gf):
+    d = parsed("small")
+    srv = gf.Server(1 << 20, max_active=2)
+    rid = srv.submit_recon(gf.Geometry(*case("small")), d["dsino"], d["norm"], 1, 1)
+    with pytest.raises(gf.GfError) as e:
+        srv.wait(rid)
+    assert e.value.status == 4
+    srv.close()
