@@ -12,6 +12,11 @@ normalization gains U(0.85, 1.15), Poisson at 5e7 counts.
   python bench.py [--gpus N --steps K --warmup W]    this library on N GPUs (replicas)
   python bench.py --impl reference ...               the CPU restatement of the
                                                      reference path (oracle), all cores
+  python bench.py --workload frames                  32 dynamic frames: one after another
+                                                     in FP32 vs one CUDA graph, FP16 storage
+  python bench.py --workload serving [--serve-seconds T]
+                                                     Poisson request stream through gf_server:
+                                                     serial FP32 vs continuous batching, FP16
 Prints one JSON line (rank 0).
 """
 from __future__ import annotations
@@ -191,6 +196,23 @@ def run_reference(args) -> int:
 
 
 # ----------------------------------------------------------------- GPU
+def max_over_ranks(x: float, dist) -> float:
+    """The slowest rank's figure (the job ends when its last replica does)."""
+    if dist is None:
+        return x
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world: int, units_per_rank: float, seconds: float) -> float:
+    """Units all replicas processed (each rank the same work) over the slowest rank's time."""
+    return world * units_per_rank / seconds
+
+
 def run_gpu(args) -> int:
     import torch
 
@@ -250,13 +272,9 @@ def run_gpu(args) -> int:
     barrier()
     clocks = clocks_stop(clk)
     launches = ctx.launches() - l0
-    ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), dist)
     subiters = NSUB * NITER * args.steps
-    value = world * subiters / (ms / 1000.0)
+    value = whole_job_rate(world, subiters, ms / 1000.0)
     stage = {}
     for name, sid in gf.STAGES.items():
         tot, n = r.profile_read(sid)
@@ -310,12 +328,8 @@ def run_gpu(args) -> int:
         for _ in range(args.e2e_steps):
             e2e_step()
         torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([dt], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dt = float(t.item())
-        e2e = {"value": world * NSUB * NITER * args.e2e_steps / dt, "unit": UNIT,
+        dt = max_over_ranks(time.perf_counter() - t0, dist)
+        e2e = {"value": whole_job_rate(world, NSUB * NITER * args.e2e_steps, dt), "unit": UNIT,
                "h2d_bytes_per_step": (n2 + ndata) * 4, "d2h_bytes_per_step": nvox * 4,
                "steps": args.e2e_steps, "ms_per_step": 1000.0 * dt / args.e2e_steps,
                "path": "gf_recon_load(pinned host sinogram+normalization) + gf_recon_iterate(2) + "
@@ -347,6 +361,279 @@ def run_gpu(args) -> int:
     return 0
 
 
+# ----------------------------------------------------------------- other workloads
+def ellipsoid_phantom(res: int, nzs: int, seed: int, norgans: int = 6) -> tuple:
+    """Body ellipsoid and hot organ ellipsoids scaled to the image, [NZS][RES][RES]:
+    returns (body without organs, organs at their contrast)."""
+    rs = np.random.RandomState(seed)
+    z, y, x = np.meshgrid(np.arange(nzs, dtype=np.float32), np.arange(res, dtype=np.float32),
+                          np.arange(res, dtype=np.float32), indexing="ij")
+    c, cz = (res - 1) / 2.0, (nzs - 1) / 2.0
+    ax, ay, az = 0.31 * res, 0.23 * res, 0.44 * nzs
+    body = ((x - c) / ax) ** 2 + ((y - c) / ay) ** 2 + ((z - cz) / az) ** 2 <= 1.0
+    organs = np.zeros_like(x)
+    for _ in range(norgans):
+        ox, oy, oz = rs.uniform(-0.6, 0.6) * ax, rs.uniform(-0.6, 0.6) * ay, rs.uniform(-0.7, 0.7) * az
+        sx, sy, sz = rs.uniform(0.07, 0.2) * ax, rs.uniform(0.07, 0.2) * ay, rs.uniform(0.05, 0.15) * az
+        o = ((x - c - ox) / sx) ** 2 + ((y - c - oy) / sy) ** 2 + ((z - cz - oz) / sz) ** 2 <= 1.0
+        organs = np.where(o & body, rs.uniform(2.0, 20.0), organs)
+    bg = np.where(body & (organs == 0), 1.0, 0.0).astype(np.float32)
+    return bg.ravel(), organs.astype(np.float32).ravel()
+
+
+def project(gf, ctx, img: np.ndarray):
+    """Full projection of a [NZS][RES][RES] image with the library's projector, left on the device."""
+    import torch
+
+    d = ctx.put(img)
+    out = torch.zeros(ctx.ndata, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()  # the library's stream does not wait for torch's
+    arr = gf.DeviceArray.view(ctx, out.data_ptr(), ctx.ndata)
+    for s in range(ctx.nsub):
+        ctx.forward_project(d, s, arr)
+    ctx.sync()
+    d.free()
+    return out
+
+
+def noisy_sinogram(lam, gains, counts: float, seed: int):
+    """Prompts ~ Poisson(lam * gains scaled to `counts`), background 0; (dsino, norm) on the host."""
+    import torch
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    m = lam * gains
+    m = m * (counts / float(m.sum()))
+    prompts = torch.poisson(m, generator=g)
+    dsino = np.zeros(2 * lam.numel(), np.float32)
+    dsino[: lam.numel()] = prompts.cpu().numpy()
+    return dsino, gains.cpu().numpy()
+
+
+def gpu_gains(n: int, seed: int):
+    import torch
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    return 0.85 + 0.3 * torch.rand(n, generator=g, device="cuda")
+
+
+def run_frames(args) -> int:
+    """32 dynamic frames at the preclinical geometry.  Seeded two-compartment
+    time-activity curves (blood-like washout in the body, uptake in the organs)
+    shape each frame; counts are log-uniform over 1e5-5e7; each frame uses 4, 8
+    or 16 subsets and 2 iterations.  Plain: the frames one after another in FP32
+    with the default tile shapes.  Batched: FP16 storage of the ratio sinogram,
+    autotuned tile shapes, every frame's iteration replayed from one CUDA graph
+    (frames run as parallel branches); batched_f32 the same in FP32 storage.
+    Data resident in HBM in every arm."""
+    import torch
+
+    import gfirst_gb300 as gf
+
+    torch.cuda.set_device(0)
+    nf, niter = args.frames, 2
+    rs = np.random.RandomState(2024)
+    nsubs = rs.choice([4, 8, 16], nf)
+    counts = np.exp(rs.uniform(np.log(1e5), np.log(5e7), nf))
+    t = np.cumsum(np.geomspace(0.5, 6.0, nf))  # frame mid-times, minutes
+    blood = 1.0 + 9.0 * np.exp(-t / 1.5)
+    uptake = 1.0 - np.exp(-t / 12.0)
+    g = gf.Geometry(*GEOM)
+    c0 = gf.Context(g, nsub=16)
+    bg, organs = ellipsoid_phantom(GEOM[0], GEOM[1], 7, norgans=10)
+    pb, po = project(gf, c0, bg), project(gf, c0, organs)
+    c0.close()
+    gains = gpu_gains(pb.numel(), 11)
+    data = []
+    for k in range(nf):
+        data.append(noisy_sinogram(blood[k] * pb + uptake[k] * po, gains, counts[k], 100 + k))
+    del pb, po, gains
+    torch.cuda.empty_cache()
+
+    def build(storage: str, tune: bool):
+        ctxs, recs, tuned = [], [], []
+        for k in range(nf):
+            c = gf.Context(g, nsub=int(nsubs[k]))
+            tuned.append(c.tune() if tune else None)
+            r = gf.Recon(c, 1, niter=niter, storage=storage)
+            r.load(dsino=data[k][0], norm=data[k][1])
+            r._keep = None
+            ctxs.append(c)
+            recs.append(r)
+        return ctxs, recs, tuned
+
+    subiters = int(sum(int(s) * niter for s in nsubs))
+    out = {}
+    arms = {"plain": ("f32", False), "batched_f32": ("f32", True), "batched": ("f16", True)}
+    for arm, (storage, batched) in arms.items():
+        ctxs, recs, tuned = build(storage, batched)
+        batch = gf.Batch(recs) if batched else None
+
+        def once():
+            for r in recs:
+                r.restart()
+            if batch is None:
+                for c, r in zip(ctxs, recs):  # one frame at a time
+                    r.iterate(niter)
+                    c.sync()
+            else:
+                batch.iterate(niter, graph=True)
+                batch.sync()
+
+        for _ in range(args.warmup):
+            once()
+        l0 = sum(c.launches() for c in ctxs)
+        clk = clocks_start(0)
+        time.sleep(0.3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            once()
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / args.steps
+        clocks = clocks_stop(clk)
+        launches = (sum(c.launches() for c in ctxs) - l0) // args.steps
+        img0 = recs[0].image()
+        out[arm] = {"ms_per_step": 1000.0 * dt, "subiters_per_s": subiters / dt, "frames_per_s": nf / dt,
+                    "storage": storage, "graph": batched,
+                    "gpu_launches_per_step": launches, "clocks": clocks,
+                    "tuned": sorted({json.dumps(x, sort_keys=True) for x in tuned if x}) or None,
+                    "frame0_image_sum": float(img0.astype(np.float64).sum())}
+        if batch is not None:
+            batch.close()
+        for r in recs:
+            r.close()
+        for c in ctxs:
+            c.close()
+    rel = abs(out["batched"]["frame0_image_sum"] / out["plain"]["frame0_image_sum"] - 1.0)
+    line = {"metric": METRIC, "value": out["batched"]["subiters_per_s"], "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["batched"]["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 arithmetic",
+            "data": "synthetic: seeded body + 10 organs, two-compartment curves, gains U(0.85,1.15), Poisson",
+            "config": {"workload": f"{nf} dynamic frames, preclinical geometry (128x128x159, 128x160x4319), "
+                                   f"{niter} iterations, subsets per frame in {{4,8,16}}",
+                       "subsets": [int(x) for x in nsubs], "counts": [float(x) for x in counts],
+                       "subiterations_per_step": subiters,
+                       "step": "every frame restarted from the cylinder and reconstructed, data resident"},
+            "arms": out, "speedup_batched_vs_plain": out["batched"]["subiters_per_s"] / out["plain"]["subiters_per_s"],
+            "speedup_batched_f32_vs_plain": out["batched_f32"]["subiters_per_s"] / out["plain"]["subiters_per_s"],
+            "frame0_sum_rel_diff_f16_vs_f32": rel}
+    print(json.dumps(line))
+    return 0
+
+
+SERVE_SIZES = {
+    "64^3": ((64, 64, 64, 64, 3, 21, 1.6, 84.8772096, 51.2), 8),
+    "96^3": ((96, 96, 96, 96, 3, 31, 1.6, 127.3158, 76.8), 8),
+    "128x128x159": (GEOM, 16),
+}
+
+
+def run_serving(args) -> int:
+    """Poisson request stream through gf_server.  Arrivals at 20/s (seeded);
+    sizes uniform over 64^3, 96^3 and 128x128x159 voxels; a quarter are bare
+    forward projections of seeded ellipsoid phantoms, the rest reconstructions
+    of 2 or 3 iterations with counts log-uniform over 1e5-5e7 (drawn from a
+    pool of 6 pre-generated noisy sinograms per size).  HBM budget 150 GB.
+    Plain: FP32, one request at a time.  Batched: FP16 storage of the ratio
+    sinogram, up to 8 requests in flight (continuous batching).  Latency runs
+    from submission to the result in host memory."""
+    import threading
+
+    import torch
+
+    import gfirst_gb300 as gf
+
+    torch.cuda.set_device(0)
+    rs = np.random.RandomState(77)
+    pool = {}
+    for name, (geo, nsub) in SERVE_SIZES.items():
+        g = gf.Geometry(*geo)
+        c = gf.Context(g, nsub=nsub)
+        bg, organs = ellipsoid_phantom(geo[0], geo[1], 31, norgans=6)
+        lam = project(gf, c, bg + organs)
+        c.close()
+        gains = gpu_gains(lam.numel(), 32)
+        lv = np.exp(rs.uniform(np.log(1e5), np.log(5e7), 6))
+        sinos = [noisy_sinogram(lam, gains, float(x), 40 + i) for i, x in enumerate(lv)]
+        imgs = []
+        for i in range(4):
+            b, o = ellipsoid_phantom(geo[0], geo[1], 50 + i)
+            imgs.append(b + o)
+        pool[name] = (g, nsub, sinos, imgs, [float(x) for x in lv])
+        del lam, gains
+    torch.cuda.empty_cache()
+    names = list(SERVE_SIZES)
+    n = int(rs.poisson(args.serve_rate * args.serve_seconds))
+    arrivals = np.sort(rs.uniform(0.0, args.serve_seconds, n))
+    reqs = []
+    for i in range(n):
+        nm = names[rs.randint(3)]
+        if rs.rand() < 0.25:
+            reqs.append(("project", nm, rs.randint(4), 0))
+        else:
+            reqs.append(("recon", nm, rs.randint(6), 2 + rs.randint(2)))
+    budget = 150 * 10**9
+    out = {}
+    for arm, storage, max_active in (("plain", "f32", 1), ("batched", "f16", 8)):
+        srv = gf.Server(budget, max_active=max_active)
+        ids = [None] * n
+        ready = threading.Event()
+        t_start = [0.0]
+
+        def submitter():
+            t0 = time.perf_counter()
+            t_start[0] = t0
+            ready.set()
+            for i, (kind, nm, k, it) in enumerate(reqs):
+                d = arrivals[i] - (time.perf_counter() - t0)
+                if d > 0:
+                    time.sleep(d)
+                g, nsub, sinos, imgs, _ = pool[nm]
+                if kind == "project":
+                    ids[i] = srv.submit_project(g, imgs[k], nsub)
+                else:
+                    ids[i] = srv.submit_recon(g, sinos[k][0], sinos[k][1], nsub, it, storage)
+
+        clk = clocks_start(0)
+        th = threading.Thread(target=submitter)
+        th.start()
+        ready.wait()
+        lat = {"project": [], "recon": []}
+        for i in range(n):
+            while ids[i] is None:
+                time.sleep(0.0005)
+            _, ms = srv.wait(ids[i])
+            lat[reqs[i][0]].append(ms)
+        t_end = time.perf_counter()
+        th.join()
+        clocks = clocks_stop(clk)
+        st = srv.stats()
+        srv.close()
+        by_kind = {k: {"n": len(v), "p50_ms": float(np.percentile(v, 50)), "p99_ms": float(np.percentile(v, 99))}
+                   for k, v in lat.items() if v}
+        out[arm] = {"storage": storage, "max_active": max_active, "completed": st["completed"],
+                    "failed": st["failed"], "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                    "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
+                    "throughput_per_s": st["completed"] / (t_end - t_start[0]),
+                    "makespan_s": t_end - t_start[0], "peak_active": st["peak_active"],
+                    "mean_queue_ms": st["queue_ms"], "mean_load_ms": st["load_ms"], "mean_run_ms": st["run_ms"],
+                    "peak_bytes": st["peak_bytes"], "by_kind": by_kind, "clocks": clocks}
+    line = {"metric": "requests/s", "value": out["batched"]["throughput_per_s"], "unit": "req/s", "n_gpus": 1,
+            "steps": n, "warmup": 0, "ms_per_step": out["batched"]["mean_ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 arithmetic",
+            "data": "synthetic: seeded ellipsoid phantoms, gains U(0.85,1.15), Poisson",
+            "config": {"workload": f"Poisson request stream, {args.serve_rate:g} req/s for {args.serve_seconds:g} s, "
+                                   "sizes 64^3 / 96^3 / 128x128x159, 25% bare projections, "
+                                   "2-3 iterations, HBM budget 150 GB",
+                       "requests": n, "subsets": {k: v[1] for k, v in SERVE_SIZES.items()},
+                       "count_levels": {k: pool[k][4] for k in names}},
+            "arms": out}
+    print(json.dumps(line))
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -355,9 +642,17 @@ def main() -> int:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--workload", default="recon", choices=["recon", "frames", "serving"])
+    ap.add_argument("--frames", type=int, default=32)
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "frames":
+        return run_frames(args)
+    if args.workload == "serving":
+        return run_serving(args)
     return run_gpu(args)
 
 

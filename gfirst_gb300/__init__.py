@@ -141,6 +141,17 @@ class DeviceArray:
         p = ctypes.c_void_p()
         _ck(lib().gf_device_alloc(ctx.h, self.nbytes, ctypes.byref(p)))
         self.p = p
+        self._owned = True
+
+    @classmethod
+    def view(cls, ctx: "Context", ptr: int, n: int, dtype=np.float32) -> "DeviceArray":
+        """Borrow device memory allocated elsewhere (e.g. a torch tensor's data_ptr());
+        never freed here."""
+        a = cls.__new__(cls)
+        a.ctx, a.n, a.dtype = ctx, int(n), np.dtype(dtype)
+        a.p = ctypes.c_void_p(int(ptr))
+        a._owned = False
+        return a
 
     @property
     def nbytes(self) -> int:
@@ -161,9 +172,9 @@ class DeviceArray:
         return self.upload(np.zeros(self.n, self.dtype))
 
     def free(self) -> None:
-        if self.p:
+        if self.p and self._owned:
             lib().gf_device_free(self.ctx.h, self.p)
-            self.p = ctypes.c_void_p()
+        self.p = ctypes.c_void_p()
 
     def __del__(self):
         try:
@@ -288,6 +299,9 @@ class Recon:
     def iterate(self, n: int = 1) -> None:
         _ck(lib().gf_recon_iterate(self.h, n))
 
+    def restart(self) -> None:
+        _ck(lib().gf_recon_restart(self.h))
+
     def subiteration(self) -> None:
         _ck(lib().gf_recon_subiteration(self.h))
 
@@ -353,7 +367,8 @@ class _CServerStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int64) for n in ("submitted", "completed", "failed", "queued", "active")] + \
                [(n, ctypes.c_double) for n in ("p50_ms", "p99_ms", "mean_ms", "max_ms", "throughput_per_s")] + \
                [(n, ctypes.c_int64) for n in ("bytes_in_use", "peak_bytes", "budget_bytes")] + \
-               [("peak_active", ctypes.c_int32)]
+               [("peak_active", ctypes.c_int32)] + \
+               [(n, ctypes.c_double) for n in ("queue_ms", "load_ms", "run_ms")]
 
 
 class Server:

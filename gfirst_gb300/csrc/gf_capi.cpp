@@ -70,12 +70,13 @@ using namespace gf;
 
 // ---------------------------------------------------------------- context
 gf_status gf_ctx::alloc(size_t bytes, void** p) {
+  // stream-ordered: no device-wide synchronisation when contexts come and go
   *p = nullptr;
   if (bytes == 0) bytes = 16;
-  cudaError_t e = cudaMalloc(p, bytes);
+  cudaError_t e = cudaMallocAsync(p, bytes, stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
-    return cuda_error(e, "cudaMalloc");
+    return cuda_error(e, "cudaMallocAsync");
   }
   owned.push_back(DevBuf{*p, bytes});
   return GF_OK;
@@ -207,6 +208,17 @@ gf_status gf_create(const gf_geometry* g, int32_t nsubsets, int32_t device, gf_c
   if (const char* v = getenv("GF_FP_LC")) lc = atoi(v);
   if (!make_fp_schedule(plan, R, lc, &fps)) return set_error(GF_ERR_GEOMETRY, "no forward-projector schedule fits");
 
+  {
+    // keep memory returned by cudaFreeAsync cached in the device's pool, so
+    // reconstructions created after others finish reuse it without a round
+    // trip to the driver (process-local setting)
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+  }
   gf_ctx* c = new gf_ctx();
   c->plan = std::move(plan);
   c->fps = std::move(fps);
@@ -241,11 +253,11 @@ gf_status gf_create(const gf_geometry* g, int32_t nsubsets, int32_t device, gf_c
   if ((st = c->alloc_t(trig.size(), &c->d_trig)) != GF_OK) return fail(st);
   if ((st = c->alloc_t(rowmap.size(), &c->d_rowmap)) != GF_OK) return fail(st);
   if ((st = c->alloc_t(512, &c->d_runs)) != GF_OK) return fail(st);  // room for any schedule (<= 512 threads)
-  cudaMemcpy(c->d_seg, segs.data(), segs.size() * sizeof(DevSeg), cudaMemcpyHostToDevice);
-  cudaMemcpy(c->d_trig, trig.data(), trig.size() * sizeof(float2), cudaMemcpyHostToDevice);
-  cudaMemcpy(c->d_rowmap, rowmap.data(), rowmap.size() * sizeof(int2), cudaMemcpyHostToDevice);
-  if ((e = cudaMemcpy(c->d_runs, runs.data(), runs.size() * sizeof(int4), cudaMemcpyHostToDevice)) != cudaSuccess)
-    return fail(cuda_error(e, "cudaMemcpy tables"));
+  cudaMemcpyAsync(c->d_seg, segs.data(), segs.size() * sizeof(DevSeg), cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(c->d_trig, trig.data(), trig.size() * sizeof(float2), cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(c->d_rowmap, rowmap.data(), rowmap.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(c->d_runs, runs.data(), runs.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream);
+  if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return fail(cuda_error(e, "table upload"));
   DevGeom& d = c->dg;
   d.res = p.g.res; d.nzs = p.g.nzs; d.nrad = p.g.nrad; d.nang = p.g.nang; d.nseg = p.g.nseg; d.nzp = p.NZP;
   d.P = p.P; d.PP = p.PP; d.PS = p.PS; d.nsub = p.nsub;
@@ -260,8 +272,8 @@ gf_status gf_create(const gf_geometry* g, int32_t nsubsets, int32_t device, gf_c
 void gf_destroy(gf_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
+  for (auto& b : c->owned) cudaFreeAsync(b.p, c->stream);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  for (auto& b : c->owned) cudaFree(b.p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

@@ -22,10 +22,10 @@ using namespace gf;
 
 gf_status gf_recon::alloc(size_t bytes, void** q) {
   *q = nullptr;
-  cudaError_t e = cudaMalloc(q, bytes ? bytes : 16);
+  cudaError_t e = cudaMallocAsync(q, bytes ? bytes : 16, ctx->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
-    return cuda_error(e, "cudaMalloc (reconstruction)");
+    return cuda_error(e, "cudaMallocAsync (reconstruction)");
   }
   owned.push_back(DevBuf{*q, bytes});
   return GF_OK;
@@ -194,12 +194,12 @@ gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out)
 
 void gf_recon_destroy(gf_recon* r) {
   if (!r) return;
-  if (r->ctx) cudaStreamSynchronize(r->ctx->stream);
+  for (auto& b : r->owned) cudaFreeAsync(b.p, r->ctx->stream);
+  cudaStreamSynchronize(r->ctx->stream);
   for (auto& e : r->evs) {
     cudaEventDestroy(e.a);
     cudaEventDestroy(e.b);
   }
-  for (auto& b : r->owned) cudaFree(b.p);
   delete r;
 }
 
@@ -334,12 +334,12 @@ gf_status gf_recon_get_image(gf_recon* r, int32_t type, int32_t scaled, float* h
   gf_ctx* c = r->ctx;
   const Plan& pl = c->plan;
   float* tmp = nullptr;
-  GF_CK(cudaMalloc(&tmp, pl.nvox * sizeof(float)));
+  GF_CK(cudaMallocAsync(&tmp, pl.nvox * sizeof(float), c->stream));
   const float scale = type == 0 ? r->p.scale_d : r->p.scale_t;
   cudaError_t e = launch_zfast_to_file(c->dg, r->img[type], scale, scaled ? 1 : 0, tmp, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(h_out, tmp, pl.nvox * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  cudaFreeAsync(tmp, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  cudaFree(tmp);
   if (e != cudaSuccess) return cuda_error(e, "get image");
   return GF_OK;
 }

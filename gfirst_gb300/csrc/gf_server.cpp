@@ -2,16 +2,19 @@
 // batching on one device.
 //
 // Requests (reconstructions and bare projections, of any geometry) wait in
-// arrival order.  A worker thread admits the head of the queue when its
+// arrival order.  A loader thread admits the head of the queue when its
 // device bytes (gf_recon_bytes) fit the remaining budget and fewer than
 // max_active requests run, builds its context (own stream) and
-// reconstruction, and loads its data.  Every active reconstruction keeps one
-// iteration in flight: when its completion event fires the next iteration is
-// queued, so requests of different sizes advance independently and their
-// kernels overlap on the device.  A finished request's image is read back,
-// its memory released, and the queue re-examined.  Results do not depend on
-// what else runs: each request owns its buffers and the kernels are
-// deterministic for modes 0 and 1.
+// reconstruction, and loads its data; a projection is answered right there.
+// A worker thread keeps one iteration in flight for every loaded
+// reconstruction: when its completion event fires the next iteration is
+// queued, so requests of different sizes advance independently, their
+// kernels overlap on the device, and loading a new request does not stall
+// the running ones.  A finished request's image is read back, its memory
+// returned (stream-ordered, to the device's pool), and the loader
+// re-examines the queue.  Results do not depend on what else runs: each
+// request owns its buffers and the kernels are deterministic for modes 0
+// and 1.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -35,7 +38,7 @@ struct Job {
   int64_t id = 0;
   gf_request req{};
   int64_t bytes = 0;
-  double t_submit = 0, t_done = 0;
+  double t_submit = 0, t_admit = 0, t_loaded = 0, t_done = 0;
   gf_ctx* ctx = nullptr;
   gf_recon* rec = nullptr;
   cudaEvent_t ev = nullptr;
@@ -55,16 +58,18 @@ struct gf_server {
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Job*> queue;
-  std::vector<Job*> active;
+  std::vector<Job*> active;  // loaded reconstructions
+  int loading = 0;           // admitted, being set up
   std::unordered_map<int64_t, Job*> jobs;
   int64_t next_id = 1, bytes_in_use = 0, peak_bytes = 0, submitted = 0, completed = 0, failed = 0;
   int peak_active = 0;
   double t_first = -1;
   std::vector<double> lat;
   bool stop = false;
-  std::thread worker;
+  std::thread worker, loader;
 
-  void run();
+  void run();   // advances loaded reconstructions
+  void load();  // admits and sets up queued requests
   void finish(Job* j, gf_status st);
   gf_status start(Job* j);
 };
@@ -94,6 +99,7 @@ void gf_server::finish(Job* j, gf_status st) {
   }
   active.erase(std::remove(active.begin(), active.end(), j), active.end());
   cv_done.notify_all();
+  cv_work.notify_all();  // memory and a slot came free
 }
 
 gf_status gf_server::start(Job* j) {
@@ -109,55 +115,67 @@ gf_status gf_server::start(Job* j) {
   return GF_OK;
 }
 
+void gf_server::load() {
+  cudaSetDevice(device);
+  for (;;) {
+    Job* j = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      for (;;) {
+        while (!queue.empty() && queue.front()->bytes > budget) {  // can never fit
+          Job* x = queue.front();
+          queue.pop_front();
+          x->state = 2;
+          x->status = GF_ERR_NOMEM;
+          x->err = "request needs more device memory than the server's budget";
+          x->t_done = now_ms();
+          failed++;
+          cv_done.notify_all();
+        }
+        // the head waits for memory or a slot; arrival order is kept
+        if (!queue.empty() && (int)active.size() + loading < max_active && bytes_in_use + queue.front()->bytes <= budget)
+          break;
+        if (stop && queue.empty()) {
+          cv_work.notify_all();
+          return;
+        }
+        cv_work.wait(lk);
+      }
+      j = queue.front();
+      queue.pop_front();
+      bytes_in_use += j->bytes;
+      peak_bytes = std::max(peak_bytes, bytes_in_use);
+      j->state = 1;
+      j->t_admit = now_ms();
+      loading++;
+      peak_active = std::max(peak_active, (int)active.size() + loading);
+    }
+    gf_status st = start(j);
+    j->t_loaded = now_ms();
+    const bool project = j->req.kind == GF_REQ_PROJECT;
+    if (st == GF_OK && project) st = gf_recon_get_proj_ref(j->rec, j->req.h_out);
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      loading--;
+      if (st == GF_OK && !project) active.push_back(j);
+    }
+    if (st != GF_OK || project) finish(j, st);
+    cv_work.notify_all();
+  }
+}
+
 void gf_server::run() {
   cudaSetDevice(device);
   for (;;) {
-    // admission
-    std::vector<Job*> admit;
-    {
-      std::unique_lock<std::mutex> lk(mu);
-      if (queue.empty() && active.empty()) {
-        if (stop) return;
-        cv_work.wait(lk, [&] { return stop || !queue.empty(); });
-        if (queue.empty() && stop) return;
-      }
-      while (!queue.empty() && (int)active.size() + (int)admit.size() < max_active) {
-        Job* j = queue.front();
-        if (j->bytes > budget) {  // can never fit
-          queue.pop_front();
-          j->state = 2;
-          j->status = GF_ERR_NOMEM;
-          j->err = "request needs more device memory than the server's budget";
-          j->t_done = now_ms();
-          failed++;
-          cv_done.notify_all();
-          continue;
-        }
-        if (bytes_in_use + j->bytes > budget) break;  // wait for memory, keep arrival order
-        queue.pop_front();
-        bytes_in_use += j->bytes;
-        peak_bytes = std::max(peak_bytes, bytes_in_use);
-        j->state = 1;
-        admit.push_back(j);
-      }
-      for (Job* j : admit) active.push_back(j);
-      peak_active = std::max(peak_active, (int)active.size());
-    }
-    for (Job* j : admit) {
-      gf_status st = start(j);
-      if (st != GF_OK) {
-        finish(j, st);
-        continue;
-      }
-      if (j->req.kind == GF_REQ_PROJECT) finish(j, gf_recon_get_proj_ref(j->rec, j->req.h_out));
-    }
-    // progress: one iteration in flight per active reconstruction
     std::vector<Job*> act;
     {
-      std::lock_guard<std::mutex> lk(mu);
+      std::unique_lock<std::mutex> lk(mu);
+      cv_work.wait(lk, [&] { return !active.empty() || (stop && queue.empty() && loading == 0); });
+      if (active.empty()) return;
       act = active;
     }
-    bool progressed = !admit.empty();
+    // one iteration in flight per loaded reconstruction
+    bool progressed = false;
     for (Job* j : act) {
       if (j->in_flight) {
         cudaError_t e = cudaEventQuery(j->ev);
@@ -224,6 +242,7 @@ gf_status gf_server_create(int32_t device, int64_t budget, int32_t max_active, g
   s->budget = budget;
   s->max_active = max_active;
   s->worker = std::thread([s] { s->run(); });
+  s->loader = std::thread([s] { s->load(); });
   *out = s;
   return GF_OK;
 }
@@ -235,6 +254,7 @@ void gf_server_destroy(gf_server* s) {
     s->stop = true;
   }
   s->cv_work.notify_all();
+  if (s->loader.joinable()) s->loader.join();
   if (s->worker.joinable()) s->worker.join();
   for (auto& kv : s->jobs) {
     release(kv.second);
@@ -293,7 +313,7 @@ gf_status gf_server_get_stats(gf_server* s, gf_server_stats* o) {
   o->completed = s->completed;
   o->failed = s->failed;
   o->queued = (int64_t)s->queue.size();
-  o->active = (int64_t)s->active.size();
+  o->active = (int64_t)s->active.size() + s->loading;
   o->bytes_in_use = s->bytes_in_use;
   o->peak_bytes = s->peak_bytes;
   o->budget_bytes = s->budget;
@@ -308,9 +328,18 @@ gf_status gf_server_get_stats(gf_server* s, gf_server_stats* o) {
     double sum = 0;
     for (double x : l) sum += x;
     o->mean_ms = sum / (double)l.size();
-    double last = 0;
-    for (auto& kv : s->jobs)
-      if (kv.second->state == 2 && kv.second->status == GF_OK) last = std::max(last, kv.second->t_done);
+    double last = 0, q = 0, ld = 0, run = 0;
+    for (auto& kv : s->jobs) {
+      const Job* j = kv.second;
+      if (j->state != 2 || j->status != GF_OK) continue;
+      last = std::max(last, j->t_done);
+      q += j->t_admit - j->t_submit;
+      ld += j->t_loaded - j->t_admit;
+      run += j->t_done - j->t_loaded;
+    }
+    o->queue_ms = q / (double)s->completed;
+    o->load_ms = ld / (double)s->completed;
+    o->run_ms = run / (double)s->completed;
     if (last > s->t_first) o->throughput_per_s = (double)s->completed / ((last - s->t_first) / 1000.0);
   }
   return GF_OK;

@@ -43,15 +43,15 @@ extern "C" gf_status gf_tune(gf_ctx* c, int32_t* fp_run, int32_t* fp_chunk, int3
   const size_t nsub0 = (size_t)p.sub_nang[0] * p.g.nrad * p.PS;
   float2* dbg = nullptr;
   float* cal = nullptr;
-  GF_CK(cudaMalloc(&dbg, nsub0 * sizeof(float2)));
-  if (cudaMalloc(&cal, nsub0 * sizeof(float)) != cudaSuccess) {
-    cudaFree(dbg);
-    return cuda_error(cudaGetLastError(), "cudaMalloc (tune)");
+  GF_CK(cudaMallocAsync(&dbg, nsub0 * sizeof(float2), c->stream));
+  if (cudaMallocAsync(&cal, nsub0 * sizeof(float), c->stream) != cudaSuccess) {
+    cudaFreeAsync(dbg, c->stream);
+    return cuda_error(cudaGetLastError(), "cudaMallocAsync (tune)");
   }
   auto done = [&](gf_status s) {
+    cudaFreeAsync(dbg, c->stream);
+    cudaFreeAsync(cal, c->stream);
     cudaStreamSynchronize(c->stream);
-    cudaFree(dbg);
-    cudaFree(cal);
     return s;
   };
   cudaStream_t st = c->stream;

@@ -257,12 +257,16 @@ typedef struct gf_server_stats {
   double throughput_per_s;                 /* completed requests / seconds since the first submit */
   int64_t bytes_in_use, peak_bytes, budget_bytes;
   int32_t peak_active;
+  /* means over completed requests: waiting in the queue, set-up and loading
+   * (context, buffers, host->device copies), iterations and read-back */
+  double queue_ms, load_ms, run_ms;
 } gf_server_stats;
 /* A request loop on one device: requests are admitted in arrival order while
- * their device bytes fit the budget and fewer than max_active run; every
- * active request keeps one iteration in flight on its own stream, so work of
- * different requests overlaps on the device, and finished requests free
- * their memory for the queue (continuous batching). */
+ * their device bytes fit the budget and fewer than max_active run, and are
+ * set up and loaded on a loader thread; every loaded request keeps one
+ * iteration in flight on its own stream, so work of different requests
+ * overlaps on the device, and finished requests free their memory for the
+ * queue (continuous batching). */
 gf_status gf_server_create(int32_t device, int64_t budget_bytes, int32_t max_active, gf_server** out);
 /* Stops after the queued and active requests finish. */
 void gf_server_destroy(gf_server* s);
