@@ -263,7 +263,7 @@ typedef struct gf_server_stats {
 } gf_server_stats;
 /* A request loop on one device: requests are admitted in arrival order while
  * their device bytes fit the budget and fewer than max_active run, and are
- * set up and loaded on a loader thread; every loaded request keeps one
+ * set up and loaded on min(max_active, 4) loader threads; every loaded request keeps one
  * iteration in flight on its own stream, so work of different requests
  * overlaps on the device, and finished requests free their memory for the
  * queue (continuous batching). */
