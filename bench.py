@@ -14,6 +14,8 @@ normalization gains U(0.85, 1.15), Poisson at 5e7 counts.
                                                      reference path (oracle), all cores
   python bench.py --workload frames                  32 dynamic frames: one after another
                                                      in FP32 vs one CUDA graph, FP16 storage
+  python bench.py --workload triples                 mode 3 (doubles + VLOR triples), FP32/FP16/BF16
+                                                     storage, error against the FP64 oracle
   python bench.py --workload serving [--serve-seconds T]
                                                      Poisson request stream through gf_server:
                                                      serial FP32 vs continuous batching, FP16
@@ -351,7 +353,9 @@ def run_gpu(args) -> int:
                            "l2": "inputs larger than L2: each sub-iteration streams a different subset's data "
                                  "and mask (1.1 GB in all, 68 MB per sub-iteration; L2 129 MB)",
                            "parallelism": f"replicas x{world}", "subsets": NSUB, "iterations": NITER},
-                "rays_per_s": value * ndata / NSUB, "stages": stage, "roofline": roofline,
+                "rays_per_s": value * ndata / NSUB, "ray_samples_per_s": value * ndata / NSUB * (g.res + 1),
+                "voxel_views_per_s": value * nvox * (g.nang // NSUB) * g.nseg,
+                "stages": stage, "roofline": roofline,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
         print(json.dumps(line))
     r.close()
@@ -523,6 +527,111 @@ def run_frames(args) -> int:
     return 0
 
 
+def run_triples(args) -> int:
+    """Doubles + triples joint reconstruction (mode 3) at the preclinical
+    geometry.  Two seeded tracers with different ellipsoid maps; doubles =
+    Poisson of the projection of both at 4e7 counts, triples sinogram = Poisson
+    of the second tracer's projection at 2e6; 2e6 VLOR events, each a true bin
+    drawn in proportion to the second tracer's projection and a partner bin
+    drawn uniformly over the masked bins, stored as float32 LOR endpoint pairs
+    and converted on the device.  8 subsets x 3 iterations in FP32, FP16 and
+    BF16 storage of the ratio sinogram; each image's error against the FP64
+    oracle run on the host on the same inputs (test infrastructure, used only
+    as the checker)."""
+    import torch
+
+    import gfirst_gb300 as gf
+
+    torch.cuda.set_device(0)
+    nsub, niter, nev = 8, 3, args.events
+    g = gf.Geometry(*GEOM)
+    ctx = gf.Context(g, nsub=nsub)
+    bg1, org1 = ellipsoid_phantom(GEOM[0], GEOM[1], 61, norgans=10)
+    bg2, org2 = ellipsoid_phantom(GEOM[0], GEOM[1], 62, norgans=6)
+    t1, t2 = bg1 + org1, 0.3 * bg2 + org2
+    p1, p2 = project(gf, ctx, t1), project(gf, ctx, t2)
+    res = GEOM[0]
+    yy, xx = np.meshgrid(np.arange(res), np.arange(res), indexing="ij")
+    cyl = ((xx - res / 2) ** 2 + (yy - res / 2) ** 2 <= (res / 2) ** 2).astype(np.float32)
+    pblank = project(gf, ctx, np.broadcast_to(cyl, (GEOM[1], res, res)).ravel())
+    gains = gpu_gains(p1.numel(), 71)
+    dsino, norm = noisy_sinogram(p1 + p2, gains, 4e7, 72)
+    tsino, _ = noisy_sinogram(p2, gains, 2e6, 73)
+    # events: true bin ~ second tracer's projection, partner uniform over masked bins
+    rs = np.random.RandomState(74)
+    lam2 = (p2 * gains).double().cpu().numpy()
+    cdf = np.cumsum(lam2)
+    true_bins = np.searchsorted(cdf, rs.uniform(0, cdf[-1], nev), side="right")
+    masked = np.flatnonzero(pblank.cpu().numpy() > 0.01)
+    partner = masked[rs.randint(0, masked.size, nev)]
+    swap = rs.rand(nev) < 0.5
+    pairs = np.stack([np.where(swap, partner, true_bins), np.where(swap, true_bins, partner)], axis=1)
+    del lam2, cdf, p1, p2, pblank, gains
+    torch.cuda.empty_cache()
+    lors = gf.bins_endpoints(g, pairs.ravel()).reshape(nev, 12)
+    dl, de = ctx.put(lors), ctx.array(2 * nev, np.int32)
+    ctx.vlor_from_endpoints(dl, nev, de)
+    events = de.download().reshape(nev, 2)
+    dl.free()
+    de.free()
+    round_trip = bool(np.array_equal(events, pairs + 1))
+
+    out = {}
+    imgs = {}
+    for storage in ("f32", "f16", "bf16"):
+        r = gf.Recon(ctx, 3, niter=niter, storage=storage)
+        r.load(dsino=dsino, tsino=tsino, norm=norm, events=events)
+        r.iterate(1)  # warm-up
+        ctx.sync()
+        gf._ck(gf.lib().gf_recon_restart(r.h))
+        ctx.sync()
+        t0 = time.perf_counter()
+        r.iterate(niter)
+        ctx.sync()
+        dt = time.perf_counter() - t0
+        imgs[storage] = (r.image(0), r.image(1))
+        out[storage] = {"seconds": dt, "subiters_per_s": 2 * nsub * niter / dt}
+        r.close()
+    # FP64 oracle on the host (the checker)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import gfo
+
+    gfo.build()
+    t0 = time.perf_counter()
+    ref = gfo.Oracle(GEOM, "f64").recon(3, nsub=nsub, niter=niter, dsino=dsino, tsino=tsino, norm=norm, ev=events)
+    oracle_s = time.perf_counter() - t0
+    ref32 = None
+    if args.fp32_oracle:
+        ref32 = gfo.Oracle(GEOM, "f32").recon(3, nsub=nsub, niter=niter, dsino=dsino, tsino=tsino, norm=norm,
+                                               ev=events)
+
+    def rel(a, b):
+        return float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b))
+
+    for storage, (d, t) in imgs.items():
+        out[storage]["rel_l2_vs_fp64_doubles"] = rel(d, ref["img_d"])
+        out[storage]["rel_l2_vs_fp64_triples"] = rel(t, ref["img_t"])
+        if ref32 is not None:
+            out[storage]["rel_l2_vs_fp32_oracle_doubles"] = rel(d, ref32["img_d"])
+            out[storage]["rel_l2_vs_fp32_oracle_triples"] = rel(t, ref32["img_t"])
+    if ref32 is not None:  # how far the FP32 reference algorithm itself sits from FP64
+        out["fp32_oracle"] = {"rel_l2_vs_fp64_doubles": rel(ref32["img_d"], ref["img_d"]),
+                              "rel_l2_vs_fp64_triples": rel(ref32["img_t"], ref["img_t"])}
+    line = {"metric": METRIC, "value": out["f32"]["subiters_per_s"], "unit": UNIT, "n_gpus": 1, "steps": 1,
+            "warmup": 1, "ms_per_step": 1000.0 * out["f32"]["seconds"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 arithmetic",
+            "data": "synthetic: two seeded ellipsoid tracers, gains U(0.85,1.15), Poisson 4e7 / 2e6, "
+                    f"{nev} VLOR events as float32 endpoint pairs",
+            "config": {"workload": "doubles + triples joint reconstruction (mode 3), preclinical geometry, "
+                                   f"{nsub} subsets x {niter} iterations",
+                       "events": nev, "endpoint_round_trip_exact": round_trip,
+                       "step": "one reconstruction from the initial images, data resident"},
+            "arms": out, "fp64_oracle_seconds": oracle_s, "oracle_cores": gfo.cores()}
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 SERVE_SIZES = {
     "64^3": ((64, 64, 64, 64, 3, 21, 1.6, 84.8772096, 51.2), 8),
     "96^3": ((96, 96, 96, 96, 3, 31, 1.6, 127.3158, 76.8), 8),
@@ -641,8 +750,10 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--cpu-steps", type=int, default=2)
-    ap.add_argument("--workload", default="recon", choices=["recon", "frames", "serving"])
+    ap.add_argument("--cpu-steps", type=int, default=8)
+    ap.add_argument("--workload", default="recon", choices=["recon", "frames", "serving", "triples"])
+    ap.add_argument("--events", type=int, default=2_000_000)
+    ap.add_argument("--fp32-oracle", type=int, default=1, help="triples: also compare with the FP32 oracle")
     ap.add_argument("--frames", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
@@ -653,6 +764,8 @@ def main() -> int:
         return run_frames(args)
     if args.workload == "serving":
         return run_serving(args)
+    if args.workload == "triples":
+        return run_triples(args)
     return run_gpu(args)
 
 

@@ -452,6 +452,14 @@ def bin_endpoints(g: Geometry, bin_index: int) -> np.ndarray:
     return out
 
 
+def bins_endpoints(g: Geometry, bins) -> np.ndarray:
+    """Endpoints (n, 6) of the lines of response of 0-based bins."""
+    b = np.ascontiguousarray(bins, np.int64).ravel()
+    out = np.empty((b.size, 6), np.float32)
+    _ck(lib().gf_bins_endpoints(ctypes.byref(g.c()), ctypes.c_int64(b.size), _ptr(b), _ptr(out)))
+    return out
+
+
 def read_vlor_endpoints(path) -> np.ndarray:
     n = ctypes.c_int64()
     _ck(lib().gf_read_vlor_endpoints(str(path).encode(), None, ctypes.byref(n)))

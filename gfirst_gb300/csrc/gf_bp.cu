@@ -144,8 +144,8 @@ cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st) {
   if (warps < 1 || warps > 8) return cudaErrorInvalidValue;
   const int Q = a.g.nzp / 32;
   const int rmax = a.g.nzs + 2;
-  size_t smem = (size_t)warps * (a.na * sizeof(int4) + rmax * sizeof(float2));
   dim3 grid((a.g.res * a.g.res + warps - 1) / warps);
+  size_t smem = (size_t)warps * (a.na * sizeof(int4) + rmax * sizeof(float2));
   void (*k)(BpArgs, int) = nullptr;
   switch (a.storage * 16 + Q) {
 #define GF_BP_CASE(S, QQ) \
@@ -160,7 +160,7 @@ cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st) {
     default: return cudaErrorInvalidValue;
   }
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = allow_max_smem(k);
     if (e != cudaSuccess) return e;
   }
   k<<<grid, warps * 32, smem, st>>>(a, rmax);

@@ -344,12 +344,8 @@ gf_status gf_copy_to_host(gf_ctx* c, void* h, const void* d, size_t bytes) {
 }
 
 // ---------------------------------------------------------------- VLOR endpoints
-gf_status gf_bin_endpoints(const gf_geometry* gg, int64_t bin, float* out6) {
-  Geom geo;
-  if (!to_geom(gg, &geo) || !out6) return set_error(GF_ERR_ARG, "null argument");
-  Plan p;
-  std::string err;
-  if (!make_plan(geo, 1, &p, &err)) return set_error(GF_ERR_GEOMETRY, err);
+static gf_status endpoints_of(const Plan& p, int64_t bin, float* out6) {
+  const Geom& geo = p.g;
   if (bin < 0 || bin >= p.ndata) return set_error(GF_ERR_ARG, "bin out of range");
   const int64_t row = bin / ((int64_t)geo.nrad * geo.nang);
   const int t = (int)((bin / geo.nrad) % geo.nang), ird = (int)(bin % geo.nrad);
@@ -373,6 +369,20 @@ gf_status gf_bin_endpoints(const gf_geometry* gg, int64_t bin, float* out6) {
     out6[3 * k + 1] = (float)(cy - l * vx * cs);
     out6[3 * k + 2] = (float)((zt - 0.5 * geo.nzs) * hs);
   }
+  return GF_OK;
+}
+
+gf_status gf_bin_endpoints(const gf_geometry* gg, int64_t bin, float* out6) {
+  return gf_bins_endpoints(gg, 1, &bin, out6);
+}
+
+gf_status gf_bins_endpoints(const gf_geometry* gg, int64_t n, const int64_t* bins, float* out) {
+  Geom geo;
+  if (!to_geom(gg, &geo) || (n > 0 && (!bins || !out)) || n < 0) return set_error(GF_ERR_ARG, "bad argument");
+  Plan p;
+  std::string err;
+  if (!make_plan(geo, 1, &p, &err)) return set_error(GF_ERR_GEOMETRY, err);
+  for (int64_t i = 0; i < n; i++) GF_TRY(endpoints_of(p, bins[i], out + 6 * i));
   return GF_OK;
 }
 

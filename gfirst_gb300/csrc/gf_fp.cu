@@ -143,7 +143,7 @@ template <int R, bool RATIO, bool FULL, int STORE>
 static cudaError_t launch_fp_t(const FpArgs& a, const FpSchedule& s, cudaStream_t st) {
   auto k = fp_kernel<R, RATIO, FULL, STORE>;
   size_t smem = s.smem_bytes();
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = allow_max_smem(k);
   if (e != cudaSuccess) return e;
   int na = (a.g.nang - a.subset + a.g.nsub - 1) / a.g.nsub;
   dim3 grid(a.g.nrad, na);

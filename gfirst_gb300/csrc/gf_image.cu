@@ -24,6 +24,9 @@ __global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const flo
   const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int x0 = blockIdx.x * 8, y0 = blockIdx.y * 8, z = blockIdx.z * 32 + lane;
   const int RES = g.res, NZP = g.nzp;
+  // unrolled so that each warp has eight (sixteen with DIV) column loads in
+  // flight instead of one: the loop is bound by L2 latency otherwise
+#pragma unroll 8
   for (int c = ty; c < 256; c += 8) {
     const int yy = c >> 4, xx = c & 15;
     const int y = y0 - 4 + yy, x = x0 - 4 + xx;

@@ -43,6 +43,21 @@ struct BpArgs {
   int storage;             // corrcal pair type, as FpArgs::storage
 };
 cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st);
+// Lets kernel k use up to the device's opt-in shared memory per block.  Every
+// call sets the same value, so host threads that launch one kernel with
+// different shared-memory sizes at the same time cannot undo each other's
+// setting between the attribute call and the launch.
+template <class K>
+inline cudaError_t allow_max_smem(K k) {
+  static const int maxsm = [] {
+    int dev = 0, v = 48 * 1024;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return v;
+  }();
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+}
+
 
 // ---- image kernels (gf_image.cu) ----
 // out = XY PSF of `in`; with `den` the input is the update ratio in/den.

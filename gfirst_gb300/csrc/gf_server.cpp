@@ -2,8 +2,7 @@
 // batching on one device.
 //
 // Requests (reconstructions and bare projections, of any geometry) wait in
-// arrival order.  Loader threads (up to four, never more than max_active)
-// admit the head of the queue when its
+// arrival order.  A loader thread admits the head of the queue when its
 // device bytes (gf_recon_bytes) fit the remaining budget and fewer than
 // max_active requests run, builds its context (own stream) and
 // reconstruction, and loads its data; a projection is answered right there.
@@ -12,8 +11,8 @@
 // queued, so requests of different sizes advance independently, their
 // kernels overlap on the device, and loading a new request does not stall
 // the running ones.  A finished request's image is read back, its memory
-// returned (stream-ordered, to the device's pool), and the loaders
-// re-examine the queue.  Results do not depend on what else runs: each
+// returned (stream-ordered, to the device's pool), and the loader
+// re-examines the queue.  Results do not depend on what else runs: each
 // request owns its buffers and the kernels are deterministic for modes 0
 // and 1.
 #include <algorithm>
@@ -244,9 +243,9 @@ gf_status gf_server_create(int32_t device, int64_t budget, int32_t max_active, g
   s->budget = budget;
   s->max_active = max_active;
   s->worker = std::thread([s] { s->run(); });
-  // set-up and host->device copies of several requests proceed at once
-  const int nload = std::min(max_active, 4);
-  for (int i = 0; i < nload; i++) s->loaders.emplace_back([s] { s->load(); });
+  // one loader: concurrent pageable host->device copies from several threads
+  // held up the worker's launches and made every request slower
+  s->loaders.emplace_back([s] { s->load(); });
   *out = s;
   return GF_OK;
 }

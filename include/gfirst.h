@@ -157,6 +157,8 @@ gf_status gf_forward_project_noalloc(const gf_geometry* g, int32_t nsubsets, int
  * field of view.  The line is the one the forward projector samples for that
  * bin (GFIRST_GPU_Kernels.cu:75-96). */
 gf_status gf_bin_endpoints(const gf_geometry* g, int64_t bin, float* out6);
+/* The same for n bins: out holds 6 floats per bin. */
+gf_status gf_bins_endpoints(const gf_geometry* g, int64_t n, const int64_t* bins, float* out);
 /* Converts n VLOR events given as two LORs each (12 float32 per event:
  * endpoints of the first candidate LOR, then of the second) to the
  * reference's event format (int32 pairs of 1-based bins; 0 where a LOR falls
@@ -263,7 +265,7 @@ typedef struct gf_server_stats {
 } gf_server_stats;
 /* A request loop on one device: requests are admitted in arrival order while
  * their device bytes fit the budget and fewer than max_active run, and are
- * set up and loaded on min(max_active, 4) loader threads; every loaded request keeps one
+ * set up and loaded on a loader thread; every loaded request keeps one
  * iteration in flight on its own stream, so work of different requests
  * overlaps on the device, and finished requests free their memory for the
  * queue (continuous batching). */

@@ -162,6 +162,16 @@ def test_bin_endpoints_lie_on_the_detector_ring(gf, geo):
         assert abs(e[2]) < g.nzs * g.pitch and abs(e[5]) < g.nzs * g.pitch
 
 
+def test_batched_bin_endpoints_equal_single(gf):
+    g = gf.Geometry.preclinical()
+    _, ndata, _ = gf.sizes(g)
+    bins = np.random.RandomState(3).randint(0, ndata, size=500)
+    many = gf.bins_endpoints(g, bins)
+    assert np.array_equal(many, np.stack([gf.bin_endpoints(g, int(b)) for b in bins]))
+    with pytest.raises(gf.GfError):
+        gf.bins_endpoints(g, [0, ndata])  # out of range
+
+
 def test_vlor_endpoint_reader(gf, tmp_path):
     lors = np.arange(12 * 3, dtype=np.float32).reshape(3, 12)
     p = tmp_path / "v.raw"
