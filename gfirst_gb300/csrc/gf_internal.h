@@ -95,6 +95,7 @@ struct gf_recon {
   float2* dbg[2] = {nullptr, nullptr};
   float* cal = nullptr;
   float* proj_ref = nullptr;
+  bool cyl_proj_ready = false;  // proj_ref holds the unit-cylinder projection (modes 1-3)
   float* proj_t = nullptr;  // triples projection, file layout (VLOR split weights)
   int32_t* events = nullptr;
   int64_t nev = 0;

@@ -233,9 +233,13 @@ gf_status gf_recon_load(gf_recon* r, const float* h_image, const float* h_dsino,
     r->loaded = true;
     return done(GF_OK);
   }
-  // STEP 1: projection of a unit cylinder -> proj_ref (GFIRST.cu:151-184)
-  if ((s = ck(launch_cylinder(c->dg, 1.0f, r->img[0], st), "cylinder")) != GF_OK) return done(s);
-  if ((s = r->project_all(r->img[0], r->proj_ref)) != GF_OK) return done(s);
+  // STEP 1: projection of a unit cylinder -> proj_ref (GFIRST.cu:151-184).  It
+  // depends on the geometry alone, so later loads of this reconstruction keep it.
+  if (!r->cyl_proj_ready) {
+    if ((s = ck(launch_cylinder(c->dg, 1.0f, r->img[0], st), "cylinder")) != GF_OK) return done(s);
+    if ((s = r->project_all(r->img[0], r->proj_ref)) != GF_OK) return done(s);
+    r->cyl_proj_ready = true;
+  }
   // STEP 2: data (GFIRST.cu:207-260)
   float* s2 = stage;                      // 2*NDATA
   float* sn = stage + 2 * pl.ndata;       // NDATA

@@ -379,6 +379,28 @@ def _frames(gf, specs):
     return out
 
 
+def test_reload_keeps_geometry_projection_and_results(gf):
+    """A second load into the same reconstruction reuses the cylinder projection
+    and gives the same images as a fresh reconstruction of the new data."""
+    d = parsed("tinyb")
+    g = gf.Geometry(*case("tinyb"))
+    ctx = gf.Context(g, nsub=2)
+    other = dict(d, dsino=np.roll(d["dsino"], 7))
+    r = gf.Recon(ctx, 1, niter=2)
+    r.load(dsino=d["dsino"], norm=d["norm"])
+    r.iterate(2)
+    pr = r.proj_ref()
+    r.load(dsino=other["dsino"], norm=other["norm"])
+    r.iterate(2)
+    again = r.image(0)
+    assert np.array_equal(r.proj_ref(), pr)
+    fresh = gf.Recon(ctx, 1, niter=2)
+    fresh.load(dsino=other["dsino"], norm=other["norm"])
+    fresh.iterate(2)
+    assert np.array_equal(again, fresh.image(0))
+    assert np.array_equal(fresh.proj_ref(), pr)
+
+
 @pytest.mark.parametrize("graph", [True, False])
 def test_batch_matches_frames_run_alone(gf, graph):
     specs = [(1, 1), (2, 2), (1, 4), (3, 3)]
