@@ -25,10 +25,9 @@
 // (no vote), so the chunks' dependency chains interleave; lanes whose voxel
 // lies outside the segment's range are predicated off.  The floor of the axial
 // coordinate is taken with a round-down add of 1.5*2^23 instead of the
-// conversion pipe.  Counters (preclinical, 16 subsets): 1.45e9 warp
-// instructions per launch, issue 75% and load/store data pipe 73% of peak.
-#include <cstdlib>
-
+// conversion pipe.  The views of a segment run with the segment's row chunk
+// count fixed at compile time (one switch per segment), so staging issues no
+// instructions for chunks beyond the segment's rows.
 #include "gf_kernels.h"
 
 namespace gf {
@@ -45,102 +44,6 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
 
 // a + w*(b - a), the reference texture unit's linear filter in exact FP32
 __device__ __forceinline__ float2 lerp2(float2 a, float2 b, float2 w) { return __ffma2_rn(w, sub2(b, a), a); }
-
-template <int Q, int STORE>
-__global__ void __launch_bounds__(256, 4) bp_kernel(const BpArgs a, int rmax) {
-  using Pair = typename PairT<STORE>::type;
-  const Pair* cc = static_cast<const Pair*>(a.corrcal);
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const DevGeom& g = a.g;
-  const int nwarps = blockDim.x >> 5;
-  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int colidx = blockIdx.x * nwarps + wib;
-  if (colidx >= g.res * g.res) return;  // whole warp
-  const int iy = colidx / g.res, ix = colidx - iy * g.res;
-  int4* my = reinterpret_cast<int4*>(smraw) + wib * a.na;
-  float2* rows = reinterpret_cast<float2*>(reinterpret_cast<int4*>(smraw) + nwarps * a.na) + wib * rmax;
-
-  // per angle: radial texels, weight and yrot (GFIRST_GPU_Kernels.cu:136-147)
-  const float xv = __fsub_rn((float)ix, g.resm), yv = __fsub_rn((float)iy, g.resm);
-  for (int tl = lane; tl < a.na; tl += 32) {
-    const float2 sc = g.trig[subset_angle(g, a.subset, tl)];
-    const float xrot = __fadd_rn(__fmul_rn(xv, sc.y), __fmul_rn(yv, sc.x));
-    const float yrot = __fadd_rn(__fmul_rn(-xv, sc.x), __fmul_rn(yv, sc.y));
-    const float x = __fadd_rn(__fadd_rn(g.radm, __fmul_rn(xrot, g.fx_bp)), 0.5f);
-    const float xb = __fsub_rn(x, 0.5f);
-    const float fl = floorf(xb);
-    const int i = (int)fl;
-    const int i0 = clampi(i, 0, g.nrad - 1), i1 = clampi(i + 1, 0, g.nrad - 1);
-    const int rb = tl * g.nrad;
-    my[tl] = make_int4((rb + i0) * g.PS, (rb + i1) * g.PS, __float_as_int(__fsub_rn(xb, fl)), __float_as_int(yrot));
-  }
-  __syncwarp();
-
-  float fiz[Q];
-  float2 acc[Q];
-#pragma unroll
-  for (int q = 0; q < Q; q++) {
-    fiz[q] = (float)(lane + 32 * q);
-    acc[q] = make_float2(0.f, 0.f);
-  }
-
-  for (int s = 0; s < g.nseg; s++) {
-    const DevSeg sg = g.seg[s];
-    const float zlo = (float)sg.zmin, zhi = (float)(g.nzs - sg.zmin);
-    const int zm1 = sg.zmin - 1;
-    const int nrow = sg.nplanes + 2;
-    for (int tl = 0; tl < a.na; tl++) {
-      const int4 e = my[tl];
-      const float2 al2 = make_float2(__int_as_float(e.z), __int_as_float(e.z));
-      const float t = __fmul_rn(__int_as_float(e.w), sg.fz);  // yrot*fz
-      const Pair* p0 = cc + e.x + sg.blk;
-      const Pair* p1 = cc + e.y + sg.blk;
-      float2 c0[Q + 1], c1[Q + 1];
-#pragma unroll
-      for (int k = 0; k <= Q; k++) {
-        const int r = lane + 32 * k;
-        if (r < nrow) {
-          c0[k] = pair_f(__ldg(p0 + r));
-          c1[k] = pair_f(__ldg(p1 + r));
-        }
-      }
-      __syncwarp();
-#pragma unroll
-      for (int k = 0; k <= Q; k++) {
-        const int r = lane + 32 * k;
-        if (r < nrow) rows[r] = lerp2(c0[k], c1[k], al2);
-      }
-      __syncwarp();
-#pragma unroll
-      for (int q = 0; q < Q; q++) {
-        // z = float(iz) + yrot*fz + 0.5f, GFIRST_GPU_Kernels.cu:148
-        const float z = __fadd_rn(__fadd_rn(fiz[q], t), 0.5f);
-        const bool in = (lane + 32 * q < g.nzs) && z >= zlo && z < zhi;
-        if (in) {
-          const float zb = __fsub_rn(z, 0.5f);
-          // floor(zb): zb + 1.5*2^23 rounded down holds it in the low mantissa
-          // bits (|zb| < 2^22), so both the float and the integer come without
-          // a conversion instruction
-          const float y = __fadd_rd(zb, 12582912.0f);
-          const float fz = __fsub_rn(y, 12582912.0f);
-          const int j = (__float_as_int(y) - 0x4B400000) - zm1;
-          const float be = __fsub_rn(zb, fz);
-          const float2 v = lerp2(rows[j], rows[j + 1], make_float2(be, be));
-          // GFIRST_GPU_Kernels.cu:157: a negative interpolated value (a gap) zeroes both
-          if (!(v.y < 0.f || v.x < 0.f)) acc[q] = __fadd2_rn(acc[q], v);
-        }
-      }
-    }
-  }
-  float* no = a.numer + (size_t)colidx * g.nzp;
-  float* dO = a.denom + (size_t)colidx * g.nzp;
-#pragma unroll
-  for (int q = 0; q < Q; q++) {
-    const int iz = lane + 32 * q;
-    no[iz] = iz < g.nzs ? acc[q].x : 0.f;
-    dO[iz] = iz < g.nzs ? acc[q].y : 0.f;
-  }
-}
 
 // One segment's views with its row chunk count NCH fixed at compile time, so
 // the staging issues exactly the chunks the segment's rows occupy.
@@ -175,15 +78,20 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
     __syncwarp();
 #pragma unroll
     for (int q = 0; q < Q; q++) {
+      // z = float(iz) + yrot*fz + 0.5f, GFIRST_GPU_Kernels.cu:148
       const float z = __fadd_rn(__fadd_rn(fiz[q], t), 0.5f);
       const bool in = (lane + 32 * q < nzs) && z >= zlo && z < zhi;
       if (in) {
         const float zb = __fsub_rn(z, 0.5f);
+        // floor(zb): zb + 1.5*2^23 rounded down holds it in the low mantissa
+        // bits (|zb| < 2^22), so both the float and the integer come without
+        // a conversion instruction
         const float y = __fadd_rd(zb, 12582912.0f);
         const float fz = __fsub_rn(y, 12582912.0f);
         const int j = (__float_as_int(y) - 0x4B400000) - zm1;
         const float be = __fsub_rn(zb, fz);
         const float2 v = lerp2(rows[j], rows[j + 1], make_float2(be, be));
+        // GFIRST_GPU_Kernels.cu:157: a negative interpolated value (a gap) zeroes both
         if (!(v.y < 0.f || v.x < 0.f)) acc[q] = __fadd2_rn(acc[q], v);
       }
     }
@@ -191,7 +99,7 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
 }
 
 template <int Q, int STORE>
-__global__ void __launch_bounds__(256, 4) bp_seg_kernel(const BpArgs a, int rmax) {
+__global__ void __launch_bounds__(256, 4) bp_kernel(const BpArgs a, int rmax) {
   using Pair = typename PairT<STORE>::type;
   const Pair* cc = static_cast<const Pair*>(a.corrcal);
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -203,6 +111,7 @@ __global__ void __launch_bounds__(256, 4) bp_seg_kernel(const BpArgs a, int rmax
   const int iy = colidx / g.res, ix = colidx - iy * g.res;
   int4* my = reinterpret_cast<int4*>(smraw) + wib * a.na;
   float2* rows = reinterpret_cast<float2*>(reinterpret_cast<int4*>(smraw) + nwarps * a.na) + wib * rmax;
+  // per angle: radial texels, weight and yrot (GFIRST_GPU_Kernels.cu:136-147)
   const float xv = __fsub_rn((float)ix, g.resm), yv = __fsub_rn((float)iy, g.resm);
   for (int tl = lane; tl < a.na; tl += 32) {
     const float2 sc = g.trig[subset_angle(g, a.subset, tl)];
@@ -217,6 +126,7 @@ __global__ void __launch_bounds__(256, 4) bp_seg_kernel(const BpArgs a, int rmax
     my[tl] = make_int4((rb + i0) * g.PS, (rb + i1) * g.PS, __float_as_int(__fsub_rn(xb, fl)), __float_as_int(yrot));
   }
   __syncwarp();
+
   float fiz[Q];
   float2 acc[Q];
 #pragma unroll
@@ -252,10 +162,9 @@ cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st) {
   dim3 grid((a.g.res * a.g.res + warps - 1) / warps);
   size_t smem = (size_t)warps * (a.na * sizeof(int4) + rmax * sizeof(float2));
   void (*k)(BpArgs, int) = nullptr;
-  static const bool seg_variant = getenv("GF_BP_V") && atoi(getenv("GF_BP_V")) == 1;
   switch (a.storage * 16 + Q) {
 #define GF_BP_CASE(S, QQ) \
-  case S * 16 + QQ: k = seg_variant ? bp_seg_kernel<QQ, S> : bp_kernel<QQ, S>; break;
+  case S * 16 + QQ: k = bp_kernel<QQ, S>; break;
     GF_BP_CASE(0, 1) GF_BP_CASE(0, 2) GF_BP_CASE(0, 3) GF_BP_CASE(0, 4)
     GF_BP_CASE(0, 5) GF_BP_CASE(0, 6) GF_BP_CASE(0, 7) GF_BP_CASE(0, 8)
     GF_BP_CASE(1, 1) GF_BP_CASE(1, 2) GF_BP_CASE(1, 3) GF_BP_CASE(1, 4)
