@@ -45,6 +45,32 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
 // a + w*(b - a), the reference texture unit's linear filter in exact FP32
 __device__ __forceinline__ float2 lerp2(float2 a, float2 b, float2 w) { return __ffma2_rn(w, sub2(b, a), a); }
 
+// The voxels of one view: each lane's voxels interpolate between two staged
+// rows along z and add to their (NUMER, DENOM) sums.
+template <int Q>
+__device__ __forceinline__ void voxel_views(float2 (&acc)[Q], const float (&fiz)[Q], const float2* rows, float t,
+                                            float zlo, float zhi, int zm1, int nzs, int lane) {
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    // z = float(iz) + yrot*fz + 0.5f, GFIRST_GPU_Kernels.cu:148
+    const float z = __fadd_rn(__fadd_rn(fiz[q], t), 0.5f);
+    const bool in = (lane + 32 * q < nzs) && z >= zlo && z < zhi;
+    if (in) {
+      const float zb = __fsub_rn(z, 0.5f);
+      // floor(zb): zb + 1.5*2^23 rounded down holds it in the low mantissa
+      // bits (|zb| < 2^22), so both the float and the integer come without
+      // a conversion instruction
+      const float y = __fadd_rd(zb, 12582912.0f);
+      const float fz = __fsub_rn(y, 12582912.0f);
+      const int j = (__float_as_int(y) - 0x4B400000) - zm1;
+      const float be = __fsub_rn(zb, fz);
+      const float2 v = lerp2(rows[j], rows[j + 1], make_float2(be, be));
+      // GFIRST_GPU_Kernels.cu:157: a negative interpolated value (a gap) zeroes both
+      if (!(v.y < 0.f || v.x < 0.f)) acc[q] = __fadd2_rn(acc[q], v);
+    }
+  }
+}
+
 // One segment's views with its row chunk count NCH fixed at compile time, so
 // the staging issues exactly the chunks the segment's rows occupy.
 template <int Q, int NCH, class Pair>
@@ -54,46 +80,67 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
   const float zlo = (float)sg.zmin, zhi = (float)(nzs - sg.zmin);
   const int zm1 = sg.zmin - 1;
   const int nrow = sg.nplanes + 2;
-  for (int tl = 0; tl < na; tl++) {
-    const int4 e = my[tl];
-    const float2 al2 = make_float2(__int_as_float(e.z), __int_as_float(e.z));
-    const float t = __fmul_rn(__int_as_float(e.w), sg.fz);  // yrot*fz
-    const Pair* p0 = cc + e.x + sg.blk;
-    const Pair* p1 = cc + e.y + sg.blk;
-    float2 c0[NCH], c1[NCH];
+  // 16-bit pairs: the rows of view tl + 1 are loaded into the registers that
+  // view tl's rows have just left, before view tl's voxels, so their latency
+  // overlaps that work (FP16 storage 1.35 ms vs FP32 1.44 ms at the
+  // preclinical size).  FP32 pairs need twice the registers and the same
+  // pipelining made them slower (1.79 ms), so they load at the top of each view.
+  if constexpr (sizeof(Pair) == 4) {
+    Pair c0[NCH], c1[NCH];
+    auto load = [&](const int4& e) {
+      const Pair* p0 = cc + e.x + sg.blk;
+      const Pair* p1 = cc + e.y + sg.blk;
 #pragma unroll
-    for (int k = 0; k < NCH; k++) {
-      const int r = lane + 32 * k;
-      if (k < NCH - 1 || r < nrow) {
-        c0[k] = pair_f(__ldg(p0 + r));
-        c1[k] = pair_f(__ldg(p1 + r));
+      for (int k = 0; k < NCH; k++) {
+        const int r = lane + 32 * k;
+        if (k < NCH - 1 || r < nrow) {
+          c0[k] = __ldg(p0 + r);
+          c1[k] = __ldg(p1 + r);
+        }
       }
-    }
-    __syncwarp();
+    };
+    int4 e = my[0];
+    load(e);
+    for (int tl = 0; tl < na; tl++) {
+      const float2 al2 = make_float2(__int_as_float(e.z), __int_as_float(e.z));
+      const float t = __fmul_rn(__int_as_float(e.w), sg.fz);  // yrot*fz
+      __syncwarp();  // every lane is done reading the previous view's rows
 #pragma unroll
-    for (int k = 0; k < NCH; k++) {
-      const int r = lane + 32 * k;
-      if (k < NCH - 1 || r < nrow) rows[r] = lerp2(c0[k], c1[k], al2);
-    }
-    __syncwarp();
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-      // z = float(iz) + yrot*fz + 0.5f, GFIRST_GPU_Kernels.cu:148
-      const float z = __fadd_rn(__fadd_rn(fiz[q], t), 0.5f);
-      const bool in = (lane + 32 * q < nzs) && z >= zlo && z < zhi;
-      if (in) {
-        const float zb = __fsub_rn(z, 0.5f);
-        // floor(zb): zb + 1.5*2^23 rounded down holds it in the low mantissa
-        // bits (|zb| < 2^22), so both the float and the integer come without
-        // a conversion instruction
-        const float y = __fadd_rd(zb, 12582912.0f);
-        const float fz = __fsub_rn(y, 12582912.0f);
-        const int j = (__float_as_int(y) - 0x4B400000) - zm1;
-        const float be = __fsub_rn(zb, fz);
-        const float2 v = lerp2(rows[j], rows[j + 1], make_float2(be, be));
-        // GFIRST_GPU_Kernels.cu:157: a negative interpolated value (a gap) zeroes both
-        if (!(v.y < 0.f || v.x < 0.f)) acc[q] = __fadd2_rn(acc[q], v);
+      for (int k = 0; k < NCH; k++) {
+        const int r = lane + 32 * k;
+        if (k < NCH - 1 || r < nrow) rows[r] = lerp2(pair_f(c0[k]), pair_f(c1[k]), al2);
       }
+      __syncwarp();
+      if (tl + 1 < na) {
+        e = my[tl + 1];
+        load(e);
+      }
+      voxel_views<Q>(acc, fiz, rows, t, zlo, zhi, zm1, nzs, lane);
+    }
+  } else {
+    for (int tl = 0; tl < na; tl++) {
+      const int4 e = my[tl];
+      const float2 al2 = make_float2(__int_as_float(e.z), __int_as_float(e.z));
+      const float t = __fmul_rn(__int_as_float(e.w), sg.fz);  // yrot*fz
+      const Pair* p0 = cc + e.x + sg.blk;
+      const Pair* p1 = cc + e.y + sg.blk;
+      float2 c0[NCH], c1[NCH];
+#pragma unroll
+      for (int k = 0; k < NCH; k++) {
+        const int r = lane + 32 * k;
+        if (k < NCH - 1 || r < nrow) {
+          c0[k] = pair_f(__ldg(p0 + r));
+          c1[k] = pair_f(__ldg(p1 + r));
+        }
+      }
+      __syncwarp();  // every lane is done reading the previous view's rows
+#pragma unroll
+      for (int k = 0; k < NCH; k++) {
+        const int r = lane + 32 * k;
+        if (k < NCH - 1 || r < nrow) rows[r] = lerp2(c0[k], c1[k], al2);
+      }
+      __syncwarp();
+      voxel_views<Q>(acc, fiz, rows, t, zlo, zhi, zm1, nzs, lane);
     }
   }
 }

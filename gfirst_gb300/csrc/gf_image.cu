@@ -34,8 +34,9 @@ __global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const flo
     if (y >= 0 && y < RES && x >= 0 && x < RES) {
       const size_t o = ((size_t)y * RES + x) * NZP + z;
       if (DIV) {
-        const float b = den[o];
-        v = (b < 0.001f) ? 1.0f : __fdiv_rn(in[o], b);
+        // both loads unconditional, so they are in flight together
+        const float num = in[o], b = den[o];
+        v = (b < 0.001f) ? 1.0f : __fdiv_rn(num, b);
       } else {
         v = in[o];
       }
