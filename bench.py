@@ -235,6 +235,7 @@ def run_gpu(args) -> int:
 
     g = gf.Geometry(*GEOM)
     ctx = gf.Context(g, nsub=NSUB, device=local)
+    tuned = ctx.tune()  # tile shapes for this geometry, picked by timing (set-up, not timed)
     # the library queues its kernels on this stream; the CUDA events below are recorded on it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -352,7 +353,8 @@ def run_gpu(args) -> int:
                                    "data resident in HBM",
                            "l2": "inputs larger than L2: each sub-iteration streams a different subset's data "
                                  "and mask (1.1 GB in all, 68 MB per sub-iteration; L2 129 MB)",
-                           "parallelism": f"replicas x{world}", "subsets": NSUB, "iterations": NITER},
+                           "parallelism": f"replicas x{world}", "subsets": NSUB, "iterations": NITER,
+                           "tile_shapes": tuned},
                 "rays_per_s": value * ndata / NSUB, "ray_samples_per_s": value * ndata / NSUB * (g.res + 1),
                 "voxel_views_per_s": value * nvox * (g.nang // NSUB) * g.nseg,
                 "stages": stage, "roofline": roofline,

@@ -80,12 +80,12 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
   const float zlo = (float)sg.zmin, zhi = (float)(nzs - sg.zmin);
   const int zm1 = sg.zmin - 1;
   const int nrow = sg.nplanes + 2;
-  // 16-bit pairs: the rows of view tl + 1 are loaded into the registers that
-  // view tl's rows have just left, before view tl's voxels, so their latency
-  // overlaps that work (FP16 storage 1.35 ms vs FP32 1.44 ms at the
-  // preclinical size).  FP32 pairs need twice the registers and the same
-  // pipelining made them slower (1.79 ms), so they load at the top of each view.
-  if constexpr (sizeof(Pair) == 4) {
+  // The rows of view tl + 1 are loaded into the registers that view tl's rows
+  // have just left, before view tl's voxels, so their latency overlaps that
+  // work.  FP32 pairs need the larger register budget of bp_kernel's launch
+  // bounds for it (1.39 ms at 80 registers vs 1.79 ms squeezed into 64; 1.44
+  // ms without prefetch); 16-bit pairs fit in 64 (1.35 ms).
+  {
     Pair c0[NCH], c1[NCH];
     auto load = [&](const int4& e) {
       const Pair* p0 = cc + e.x + sg.blk;
@@ -117,36 +117,11 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
       }
       voxel_views<Q>(acc, fiz, rows, t, zlo, zhi, zm1, nzs, lane);
     }
-  } else {
-    for (int tl = 0; tl < na; tl++) {
-      const int4 e = my[tl];
-      const float2 al2 = make_float2(__int_as_float(e.z), __int_as_float(e.z));
-      const float t = __fmul_rn(__int_as_float(e.w), sg.fz);  // yrot*fz
-      const Pair* p0 = cc + e.x + sg.blk;
-      const Pair* p1 = cc + e.y + sg.blk;
-      float2 c0[NCH], c1[NCH];
-#pragma unroll
-      for (int k = 0; k < NCH; k++) {
-        const int r = lane + 32 * k;
-        if (k < NCH - 1 || r < nrow) {
-          c0[k] = pair_f(__ldg(p0 + r));
-          c1[k] = pair_f(__ldg(p1 + r));
-        }
-      }
-      __syncwarp();  // every lane is done reading the previous view's rows
-#pragma unroll
-      for (int k = 0; k < NCH; k++) {
-        const int r = lane + 32 * k;
-        if (k < NCH - 1 || r < nrow) rows[r] = lerp2(c0[k], c1[k], al2);
-      }
-      __syncwarp();
-      voxel_views<Q>(acc, fiz, rows, t, zlo, zhi, zm1, nzs, lane);
-    }
   }
 }
 
 template <int Q, int STORE>
-__global__ void __launch_bounds__(256, 4) bp_kernel(const BpArgs a, int rmax) {
+__global__ void __launch_bounds__(256, STORE == 0 ? 3 : 4) bp_kernel(const BpArgs a, int rmax) {
   using Pair = typename PairT<STORE>::type;
   const Pair* cc = static_cast<const Pair*>(a.corrcal);
   extern __shared__ __align__(16) unsigned char smraw[];
