@@ -54,7 +54,8 @@ __device__ __forceinline__ void voxel_views(float2 (&acc)[Q], const float (&fiz)
   for (int q = 0; q < Q; q++) {
     // z = float(iz) + yrot*fz + 0.5f, GFIRST_GPU_Kernels.cu:148
     const float z = __fadd_rn(__fadd_rn(fiz[q], t), 0.5f);
-    const bool in = (lane + 32 * q < nzs) && z >= zlo && z < zhi;
+    // every lane of chunks 0..Q-2 holds a voxel (NZP = NZS rounded up to 32)
+    const bool in = (q < Q - 1 || lane + 32 * q < nzs) && z >= zlo && z < zhi;
     if (in) {
       const float zb = __fsub_rn(z, 0.5f);
       // floor(zb): zb + 1.5*2^23 rounded down holds it in the low mantissa
