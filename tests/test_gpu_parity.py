@@ -115,6 +115,26 @@ def test_back_projection_bit_exact(gf, name, nsub, subset):
     assert np.array_equal(denom.download(), wd)
 
 
+# Axial sizes that exercise every lane-chunk count of the back projector (NZP/32
+# = 2..8), NZS a multiple of 32 or not, up to the largest NZS supported (256).
+AXIAL = [(16, nzs, 16, 12, 3, 7, 1.6, 20.7219750, 12.5) for nzs in (33, 64, 96, 130, 200, 256)]
+
+
+@pytest.mark.parametrize("geo", AXIAL, ids=lambda g: f"nzs{g[1]}")
+def test_projectors_across_axial_sizes(gf, geo):
+    o = gfo.Oracle(geo)
+    ctx = gf.Context(gf.Geometry(*geo), nsub=3)
+    corr, calib = corr_calib(o, 31)
+    numer, denom = ctx.array(o.nvox), ctx.array(o.nvox)
+    ctx.back_project(ctx.put(corr), ctx.put(calib), 1, numer, denom)
+    wn, wd = o.bp(corr, calib, 3, 1)
+    assert np.array_equal(numer.download(), wn) and np.array_equal(denom.download(), wd)
+    img = image(o, 32)
+    proj = ctx.array(o.ndata).zero()
+    ctx.forward_project(ctx.put(img), 2, proj)
+    assert rel(proj.download(), o.fp(img, 3, 2)) < FP_TOL
+
+
 # ---------------------------------------------------------------- update chain
 @pytest.mark.parametrize("name", ["tiny", "small"])
 def test_psf_and_update_bit_exact(gf, name):
