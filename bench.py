@@ -14,6 +14,8 @@ normalization gains U(0.85, 1.15), Poisson at 5e7 counts.
                                                      reference path (oracle), all cores
   python bench.py --workload frames                  32 dynamic frames: one after another
                                                      in FP32 vs one CUDA graph, FP16 storage
+  python bench.py --workload small                   the small configuration in full: GPU vs the
+                                                     CPU oracle, images against FP32/FP64 oracles
   python bench.py --workload triples                 mode 3 (doubles + VLOR triples), FP32/FP16/BF16
                                                      storage, error against the FP64 oracle
   python bench.py --workload serving [--serve-seconds T]
@@ -529,6 +531,104 @@ def run_frames(args) -> int:
     return 0
 
 
+SMALL_GEOM = (64, 32, 64, 64, 3, 11, 1.6, 84.8772096, 51.2)
+
+
+def run_small(args) -> int:
+    """The small plain-FP32 configuration, reconstructed in full on the GPU and
+    by the CPU oracle (FP32, OpenMP over the host cores) on the same inputs:
+    64x64x32 voxels of 0.8 mm, 64 radial x 64 angles x 192 planes (span 3, 11
+    segments); a water cylinder (radius 0.9 FOV/2, activity 0.1) with 6 seeded
+    ellipsoids (semi-axes 2-8 voxels, activity 0.5-5), forward-projected,
+    gains U(0.9, 1.1), Poisson at 1e6 counts; 4 subsets x 3 iterations.  The
+    images are compared with the FP32 and FP64 oracles (test infrastructure,
+    used only as the checker and the CPU baseline)."""
+    import torch
+
+    import gfirst_gb300 as gf
+
+    torch.cuda.set_device(0)
+    nsub, niter = 4, 3
+    res, nzs = SMALL_GEOM[0], SMALL_GEOM[1]
+    rs = np.random.RandomState(1001)
+    z, y, x = np.meshgrid(np.arange(nzs, dtype=np.float32), np.arange(res, dtype=np.float32),
+                          np.arange(res, dtype=np.float32), indexing="ij")
+    c = (res - 1) / 2.0
+    cyl = ((x - c) ** 2 + (y - c) ** 2) <= (0.9 * res / 2) ** 2
+    img = np.where(cyl, 0.1, 0.0).astype(np.float32)
+    for _ in range(6):
+        r = rs.uniform(0, 0.6 * res / 2)
+        ph = rs.uniform(0, 2 * np.pi)
+        ox, oy, oz = r * np.cos(ph), r * np.sin(ph), rs.uniform(-nzs / 2 + 4, nzs / 2 - 4)
+        sx, sy, sz = rs.uniform(2, 8, 3)
+        e = ((x - c - ox) / sx) ** 2 + ((y - c - oy) / sy) ** 2 + ((z - (nzs - 1) / 2 - oz) / sz) ** 2 <= 1.0
+        img = np.where(e & cyl, rs.uniform(0.5, 5.0), img).astype(np.float32)
+    g = gf.Geometry(*SMALL_GEOM)
+    ctx = gf.Context(g, nsub=nsub)
+    lam = project(gf, ctx, img.ravel()).double().cpu().numpy()
+    gains = rs.uniform(0.9, 1.1, lam.size)
+    lam = lam * gains
+    lam *= 1e6 / lam.sum()
+    dsino = np.concatenate([rs.poisson(lam), np.zeros(lam.size)]).astype(np.float32)
+    norm = gains.astype(np.float32)
+    tuned = ctx.tune()
+
+    r = gf.Recon(ctx, 1, niter=niter)
+    r.load(dsino=dsino, norm=norm)
+    for _ in range(args.warmup):
+        r.restart()
+        r.iterate(niter)
+    ctx.sync()
+    steps = max(args.steps, 1)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        r.restart()
+        r.iterate(niter)
+    ctx.sync()
+    dt = (time.perf_counter() - t0) / steps
+    gpu_img = r.image(0)
+    # end to end: load from host buffers, iterate, read the image back
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        r.load(dsino=dsino, norm=norm)
+        r.iterate(niter)
+        out_img = r.image(0)
+    e2e = (time.perf_counter() - t0) / steps
+    r.close()
+    ctx.close()
+
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import gfo
+
+    gfo.build()
+    t0 = time.perf_counter()
+    ref32 = gfo.Oracle(SMALL_GEOM, "f32").recon(1, nsub=nsub, niter=niter, dsino=dsino, norm=norm)
+    cpu_s = time.perf_counter() - t0
+    ref64 = gfo.Oracle(SMALL_GEOM, "f64").recon(1, nsub=nsub, niter=niter, dsino=dsino, norm=norm)
+
+    def rel(a, b):
+        return float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b))
+
+    subiters = nsub * niter
+    line = {"metric": METRIC, "value": subiters / dt, "unit": UNIT, "n_gpus": 1, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * dt, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded water cylinder + 6 ellipsoids, "
+            "gains U(0.9,1.1), Poisson 1e6 counts",
+            "config": {"workload": "small plain FP32 OSEM: 64x64x32 image (0.8 mm), 64 radial x 64 angles x 192 "
+                                   "planes (span 3, 11 segments), 4 subsets x 3 iterations",
+                       "step": "one full reconstruction from the cylinder, data resident", "tile_shapes": tuned},
+            "e2e": {"value": subiters / e2e, "unit": UNIT, "ms_per_step": 1000.0 * e2e,
+                    "h2d_bytes_per_step": int(dsino.nbytes + norm.nbytes), "d2h_bytes_per_step": int(out_img.nbytes)},
+            "cpu_baseline": {"value": subiters / cpu_s, "unit": UNIT, "cores": gfo.cores(), "kind": "port",
+                             "sample": "the full reconstruction (12 sub-iterations), CPU FP32 oracle, OpenMP",
+                             "seconds": cpu_s},
+            "gpu_vs_cpu_speedup": (subiters / dt) / (subiters / cpu_s),
+            "rel_l2_vs_fp32_oracle": rel(gpu_img, ref32["img_d"]), "rel_l2_vs_fp64_oracle": rel(gpu_img, ref64["img_d"]),
+            "fp32_oracle_vs_fp64": rel(ref32["img_d"], ref64["img_d"])}
+    print(json.dumps(line))
+    return 0
+
+
 def run_triples(args) -> int:
     """Doubles + triples joint reconstruction (mode 3) at the preclinical
     geometry.  Two seeded tracers with different ellipsoid maps; doubles =
@@ -753,7 +853,7 @@ def main() -> int:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=8)
-    ap.add_argument("--workload", default="recon", choices=["recon", "frames", "serving", "triples"])
+    ap.add_argument("--workload", default="recon", choices=["recon", "frames", "serving", "triples", "small"])
     ap.add_argument("--events", type=int, default=2_000_000)
     ap.add_argument("--fp32-oracle", type=int, default=1, help="triples: also compare with the FP32 oracle")
     ap.add_argument("--frames", type=int, default=32)
@@ -768,6 +868,8 @@ def main() -> int:
         return run_serving(args)
     if args.workload == "triples":
         return run_triples(args)
+    if args.workload == "small":
+        return run_small(args)
     return run_gpu(args)
 
 
