@@ -427,7 +427,8 @@ def gpu_gains(n: int, seed: int):
 
 
 def run_frames(args) -> int:
-    """32 dynamic frames at the preclinical geometry.  Seeded two-compartment
+    """32 dynamic frames at the preclinical geometry (or, with --frames-geometry
+    small, the 64x64x32 one, where one frame does not fill the GPU).  Seeded two-compartment
     time-activity curves (blood-like washout in the body, uptake in the organs)
     shape each frame; counts are log-uniform over 1e5-5e7; each frame uses 4, 8
     or 16 subsets and 2 iterations.  Plain: the frames one after another in FP32
@@ -447,9 +448,10 @@ def run_frames(args) -> int:
     t = np.cumsum(np.geomspace(0.5, 6.0, nf))  # frame mid-times, minutes
     blood = 1.0 + 9.0 * np.exp(-t / 1.5)
     uptake = 1.0 - np.exp(-t / 12.0)
-    g = gf.Geometry(*GEOM)
+    geo = GEOM if args.frames_geometry == "preclinical" else SMALL_GEOM
+    g = gf.Geometry(*geo)
     c0 = gf.Context(g, nsub=16)
-    bg, organs = ellipsoid_phantom(GEOM[0], GEOM[1], 7, norgans=10)
+    bg, organs = ellipsoid_phantom(geo[0], geo[1], 7, norgans=10)
     pb, po = project(gf, c0, bg), project(gf, c0, organs)
     c0.close()
     gains = gpu_gains(pb.numel(), 11)
@@ -519,8 +521,9 @@ def run_frames(args) -> int:
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["batched"]["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 arithmetic",
             "data": "synthetic: seeded body + 10 organs, two-compartment curves, gains U(0.85,1.15), Poisson",
-            "config": {"workload": f"{nf} dynamic frames, preclinical geometry (128x128x159, 128x160x4319), "
-                                   f"{niter} iterations, subsets per frame in {{4,8,16}}",
+            "config": {"workload": f"{nf} dynamic frames, " + ("preclinical geometry (128x128x159, 128x160x4319)"
+                                   if geo is GEOM else "small geometry (64x64x32, 64x64x192)") +
+                                   f", {niter} iterations, subsets per frame in {{4,8,16}}",
                        "subsets": [int(x) for x in nsubs], "counts": [float(x) for x in counts],
                        "subiterations_per_step": subiters,
                        "step": "every frame restarted from the cylinder and reconstructed, data resident"},
@@ -857,6 +860,7 @@ def main() -> int:
     ap.add_argument("--events", type=int, default=2_000_000)
     ap.add_argument("--fp32-oracle", type=int, default=1, help="triples: also compare with the FP32 oracle")
     ap.add_argument("--frames", type=int, default=32)
+    ap.add_argument("--frames-geometry", default="preclinical", choices=["preclinical", "small"])
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     args = ap.parse_args()
