@@ -402,9 +402,12 @@ class Server:
         return rid.value
 
     def wait(self, rid: int):
+        """Result and latency (ms) of request rid; each request is waited for once."""
         lat = ctypes.c_double()
-        _ck(lib().gf_server_wait(self.h, ctypes.c_int64(rid), ctypes.byref(lat)))
-        keep = self._keep.pop(rid)
+        try:
+            _ck(lib().gf_server_wait(self.h, ctypes.c_int64(rid), ctypes.byref(lat)))
+        finally:
+            keep = self._keep.pop(rid, None)
         return keep[-1], lat.value
 
     def stats(self) -> dict:

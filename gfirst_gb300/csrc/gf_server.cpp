@@ -20,6 +20,7 @@
 #include <condition_variable>
 #include <deque>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -64,7 +65,8 @@ struct gf_server {
   int64_t next_id = 1, bytes_in_use = 0, peak_bytes = 0, submitted = 0, completed = 0, failed = 0;
   int peak_active = 0;
   double t_first = -1;
-  std::vector<double> lat;
+  std::vector<double> lat;  // latency of every completed request
+  double sum_queue = 0, sum_load = 0, sum_run = 0, last_done = 0;
   bool stop = false;
   std::thread worker;
   std::vector<std::thread> loaders;
@@ -95,6 +97,10 @@ void gf_server::finish(Job* j, gf_status st) {
   if (st == GF_OK) {
     completed++;
     lat.push_back(j->t_done - j->t_submit);
+    sum_queue += j->t_admit - j->t_submit;
+    sum_load += j->t_loaded - j->t_admit;
+    sum_run += j->t_done - j->t_loaded;
+    last_done = std::max(last_done, j->t_done);
   } else {
     failed++;
   }
@@ -304,8 +310,16 @@ gf_status gf_server_wait(gf_server* s, int64_t id, double* latency_ms) {
   if (it == s->jobs.end()) return set_error(GF_ERR_ARG, "unknown request id");
   Job* j = it->second;
   s->cv_done.wait(lk, [&] { return j->state == 2; });
-  if (latency_ms) *latency_ms = j->t_done - j->t_submit;
-  if (j->status != GF_OK) return set_error(j->status, j->err);
+  // the request is finished and nothing else refers to it: forget it here, so
+  // a long-running server holds only requests that are queued, running or
+  // not yet waited for
+  const double lat = j->t_done - j->t_submit;
+  const gf_status st = j->status;
+  const std::string err = j->err;
+  s->jobs.erase(it);
+  delete j;
+  if (latency_ms) *latency_ms = lat;
+  if (st != GF_OK) return set_error(st, err);
   return GF_OK;
 }
 
@@ -332,19 +346,11 @@ gf_status gf_server_get_stats(gf_server* s, gf_server_stats* o) {
     double sum = 0;
     for (double x : l) sum += x;
     o->mean_ms = sum / (double)l.size();
-    double last = 0, q = 0, ld = 0, run = 0;
-    for (auto& kv : s->jobs) {
-      const Job* j = kv.second;
-      if (j->state != 2 || j->status != GF_OK) continue;
-      last = std::max(last, j->t_done);
-      q += j->t_admit - j->t_submit;
-      ld += j->t_loaded - j->t_admit;
-      run += j->t_done - j->t_loaded;
-    }
-    o->queue_ms = q / (double)s->completed;
-    o->load_ms = ld / (double)s->completed;
-    o->run_ms = run / (double)s->completed;
-    if (last > s->t_first) o->throughput_per_s = (double)s->completed / ((last - s->t_first) / 1000.0);
+    o->queue_ms = s->sum_queue / (double)s->completed;
+    o->load_ms = s->sum_load / (double)s->completed;
+    o->run_ms = s->sum_run / (double)s->completed;
+    if (s->last_done > s->t_first)
+      o->throughput_per_s = (double)s->completed / ((s->last_done - s->t_first) / 1000.0);
   }
   return GF_OK;
 }

@@ -536,4 +536,7 @@ def test_server_rejects_request_beyond_its_budget(gf):
     with pytest.raises(gf.GfError) as e:
         srv.wait(rid)
     assert e.value.status == 4
+    with pytest.raises(gf.GfError) as e:  # a finished request is forgotten once waited for
+        srv.wait(rid)
+    assert e.value.status == 1
     srv.close()
