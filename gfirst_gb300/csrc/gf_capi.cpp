@@ -272,8 +272,18 @@ gf_status gf_create(const gf_geometry* g, int32_t nsubsets, int32_t device, gf_c
 void gf_destroy(gf_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
-  for (auto& b : c->owned) cudaFreeAsync(b.p, c->stream);
+  // wait for the context's work, then return its memory on a stream of the
+  // library's own, so a caller's stream set by gf_set_stream is not needed
   if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaGetLastError();
+  cudaStream_t fs = nullptr;
+  if (cudaStreamCreateWithFlags(&fs, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    fs = nullptr;
+  }
+  for (auto& b : c->owned) cudaFreeAsync(b.p, fs);
+  cudaStreamSynchronize(fs);
+  if (fs) cudaStreamDestroy(fs);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

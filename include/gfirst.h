@@ -75,7 +75,8 @@ gf_status gf_lor_index(const gf_geometry* g, int32_t seg_ind, int32_t iz0, int32
  * loop over all angles (NSUBSETS = 1, GFIRST.h:22). */
 gf_status gf_create(const gf_geometry* g, int32_t nsubsets, int32_t device, gf_ctx** out);
 void gf_destroy(gf_ctx* ctx);
-/* Queue later work on this cudaStream_t (NULL: the context's own stream). */
+/* Queue later work on this cudaStream_t (NULL: the context's own stream).  The
+ * stream must stay valid while the context queues work on it. */
 gf_status gf_set_stream(gf_ctx* ctx, void* cuda_stream);
 gf_status gf_synchronize(gf_ctx* ctx);
 
