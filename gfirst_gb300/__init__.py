@@ -287,14 +287,19 @@ class Recon:
         except Exception:
             pass
 
-    def load(self, image=None, dsino=None, tsino=None, norm=None, events=None) -> None:
+    def load(self, image=None, dsino=None, tsino=None, norm=None, events=None, wait: bool = True) -> None:
+        """Inputs as the CLI reads them.  wait=False queues the load
+        (gf_recon_load_async): the arrays are kept referenced here until the
+        next load, and must not be modified until the context's stream has
+        passed it."""
         f32 = lambda a: None if a is None else np.ascontiguousarray(a, np.float32).ravel()  # noqa: E731
         image, dsino, tsino, norm = f32(image), f32(dsino), f32(tsino), f32(norm)
         ev = None if events is None else np.ascontiguousarray(events, np.int32)
         nev = 0 if ev is None else ev.size // 2
         self._keep = (image, dsino, tsino, norm, ev)
         p = lambda a: None if a is None else _ptr(a)  # noqa: E731
-        _ck(lib().gf_recon_load(self.h, p(image), p(dsino), p(tsino), p(norm), p(ev), ctypes.c_int64(nev)))
+        fn = lib().gf_recon_load if wait else lib().gf_recon_load_async
+        _ck(fn(self.h, p(image), p(dsino), p(tsino), p(norm), p(ev), ctypes.c_int64(nev)))
 
     def iterate(self, n: int = 1) -> None:
         _ck(lib().gf_recon_iterate(self.h, n))

@@ -203,8 +203,8 @@ void gf_recon_destroy(gf_recon* r) {
   delete r;
 }
 
-gf_status gf_recon_load(gf_recon* r, const float* h_image, const float* h_dsino, const float* h_tsino,
-                        const float* h_norm, const int32_t* h_events, int64_t nevents) {
+static gf_status load_impl(gf_recon* r, const float* h_image, const float* h_dsino, const float* h_tsino,
+                           const float* h_norm, const int32_t* h_events, int64_t nevents, bool wait) {
   if (!r) return set_error(GF_ERR_ARG, "null reconstruction");
   gf_ctx* c = r->ctx;
   const Plan& pl = c->plan;
@@ -221,7 +221,7 @@ gf_status gf_recon_load(gf_recon* r, const float* h_image, const float* h_dsino,
   if (!r->stage) GF_TRY(r->alloc_t(stage_n, &r->stage));
   float* stage = r->stage;
   auto done = [&](gf_status s) {
-    cudaStreamSynchronize(st);
+    if (wait || s != GF_OK) cudaStreamSynchronize(st);
     return s;
   };
   auto ck = [&](cudaError_t e, const char* w) { return e == cudaSuccess ? GF_OK : cuda_error(e, w); };
@@ -265,6 +265,16 @@ gf_status gf_recon_load(gf_recon* r, const float* h_image, const float* h_dsino,
   if ((s = r->init_images()) != GF_OK) return done(s);
   r->loaded = true;
   return done(GF_OK);
+}
+
+gf_status gf_recon_load(gf_recon* r, const float* h_image, const float* h_dsino, const float* h_tsino,
+                        const float* h_norm, const int32_t* h_events, int64_t nevents) {
+  return load_impl(r, h_image, h_dsino, h_tsino, h_norm, h_events, nevents, true);
+}
+
+gf_status gf_recon_load_async(gf_recon* r, const float* h_image, const float* h_dsino, const float* h_tsino,
+                              const float* h_norm, const int32_t* h_events, int64_t nevents) {
+  return load_impl(r, h_image, h_dsino, h_tsino, h_norm, h_events, nevents, false);
 }
 
 gf_status gf_recon_restart(gf_recon* r) {

@@ -199,6 +199,13 @@ void gf_recon_destroy(gf_recon* r);
  * (GFIRST.cu:207-288).  Mode 0 takes h_image (NVOX floats) instead. */
 gf_status gf_recon_load(gf_recon* r, const float* h_image, const float* h_dsino, const float* h_tsino,
                         const float* h_norm, const int32_t* h_events, int64_t nevents);
+/* The same work queued on the context's stream without waiting for it (no
+ * counterpart in the reference): the host buffers must stay untouched until
+ * the stream has passed the load (gf_synchronize, or a call that returns
+ * host results such as gf_recon_get_image).  With two reconstructions on two
+ * contexts, the next data set loads while the current one iterates. */
+gf_status gf_recon_load_async(gf_recon* r, const float* h_image, const float* h_dsino, const float* h_tsino,
+                              const float* h_norm, const int32_t* h_events, int64_t nevents);
 /* Back to the initial images of GFIRST.cu:282-288 (and the initial triples
  * projection of mode 3) without reloading the data; progress restarts at 0. */
 gf_status gf_recon_restart(gf_recon* r);

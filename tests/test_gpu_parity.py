@@ -399,6 +399,30 @@ def _frames(gf, specs):
     return out
 
 
+def test_async_load_on_two_streams_matches_sync_load(gf):
+    """Two reconstructions on two contexts, loads queued without waiting and
+    interleaved with the other's iterations, give the images of plain loads."""
+    d = parsed("tinyb")
+    g = gf.Geometry(*case("tinyb"))
+    other = np.roll(d["dsino"], 11)
+    ref = []
+    for ds in (d["dsino"], other):
+        c = gf.Context(g, nsub=2)
+        r = gf.Recon(c, 1, niter=2)
+        r.load(dsino=ds, norm=d["norm"])
+        r.iterate(2)
+        ref.append(r.image(0))
+    ca, cb = gf.Context(g, nsub=2), gf.Context(g, nsub=2)
+    ra, rb = gf.Recon(ca, 1, niter=2), gf.Recon(cb, 1, niter=2)
+    for _ in range(2):
+        ra.load(dsino=d["dsino"], norm=d["norm"], wait=False)
+        ra.iterate(2)
+        rb.load(dsino=other, norm=d["norm"], wait=False)
+        rb.iterate(2)
+        assert np.array_equal(ra.image(0), ref[0])
+        assert np.array_equal(rb.image(0), ref[1])
+
+
 def test_reload_keeps_geometry_projection_and_results(gf):
     """A second load into the same reconstruction reuses the cylinder projection
     and gives the same images as a fresh reconstruction of the new data."""
