@@ -248,6 +248,39 @@ def test_recon_with_subsets_matches_oracle(gf, mode, nsub):
         assert abs(rel(got, exact[key]) - rel(want[key], exact[key])) < IMG_TOL
 
 
+@pytest.mark.parametrize("case_", ["zero_data", "zero_events", "zero_norm_rows"])
+def test_recon_edge_inputs_match_oracle(gf, case_):
+    """Inputs at the edges of what the reference reads: an all-zero sinogram
+    (every ratio 0, the image collapses), mode 3 with no VLOR events, and a
+    normalization with whole rows of zeros (masked bins)."""
+    geo = case("tinyb")
+    d = parsed("tinyb")
+    mode, nsub = 1, 3
+    dsino, norm, events = d["dsino"].copy(), d["norm"].copy(), d["events"]
+    if case_ == "zero_data":
+        dsino[:] = 0.0
+    elif case_ == "zero_events":
+        mode, events = 3, np.zeros((0, 2), np.int32)
+    else:
+        nrad = geo[2]
+        rows = norm.reshape(-1, nrad)
+        rows[::7] = 0.0
+    o = gfo.Oracle(geo)
+    want = o.recon(mode, nsub=nsub, niter=2, dsino=dsino, tsino=d["tsino"], norm=norm, ev=events)
+    ctx = gf.Context(gf.Geometry(*geo), nsub=nsub)
+    r = gf.Recon(ctx, mode, niter=2)
+    r.load(dsino=dsino, tsino=d["tsino"] if mode >= 2 else None, norm=norm, events=events if mode == 3 else None)
+    r.iterate(2)
+    for t, key in ((0, "img_d"), (1, "img_t")):
+        if mode == 1 and t == 1:
+            continue
+        got, ref = r.image(t), want[key]
+        if np.linalg.norm(ref) == 0:
+            assert np.array_equal(got, ref)
+        else:
+            assert rel(got, ref) < IMG_TOL
+
+
 def test_recon_small_geometry_mode1_subsets(gf):
     geo = case("small")
     d = parsed("small")
