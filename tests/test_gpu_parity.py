@@ -352,6 +352,24 @@ def test_preclinical_back_projection_subset_bit_exact(gf, c2):
     assert np.array_equal(numer.download(), wn) and np.array_equal(denom.download(), wd)
 
 
+def test_reference_geometry_projectors_match_oracle(gf):
+    """The geometry compiled into the reference (GFIRST.h: 147 radial bins, 168
+    angles, span 11, 15 segments, 1293 planes): projection of one subset within
+    tolerance, back projection bit for bit."""
+    g = gf.Geometry.reference()
+    o = gfo.Oracle(g.tuple())
+    ctx = gf.Context(g, nsub=16)
+    img = image(o, 41)
+    proj = ctx.array(o.ndata).zero()
+    ctx.forward_project(ctx.put(img), 5, proj)
+    assert rel(proj.download(), o.fp(img, 16, 5)) < FP_TOL
+    corr, calib = corr_calib(o, 42)
+    numer, denom = ctx.array(o.nvox), ctx.array(o.nvox)
+    ctx.back_project(ctx.put(corr), ctx.put(calib), 5, numer, denom)
+    wn, wd = o.bp(corr, calib, 16, 5)
+    assert np.array_equal(numer.download(), wn) and np.array_equal(denom.download(), wd)
+
+
 def test_preclinical_properties(gf, c2):
     """Size-independent checks on the full 128x128x159 / 4319-plane geometry."""
     g, ctx = c2
