@@ -308,6 +308,21 @@ def run_gpu(args) -> int:
                    "ms_per_launch": stage[k]["ms_per_launch"], "peak_source": f"{peak_src} hbm_gbs"}
     roofline = dict(roof[dom], kernel=dom)
     roofline["other"] = {k: v for k, v in roof.items() if k != dom}
+    # the projectors are bound on chip: instruction issue against the SMs'
+    # peak (4 warp instructions per SM per cycle at the sampled clock), from
+    # the warp-instruction count ncu measured per launch and the live duration
+    props = torch.cuda.get_device_properties(local)
+    onchip = {}
+    for k in ("fp", "bp"):
+        ins = traffic.get(k, {}).get("warp_instructions")
+        if k in stage and ins:
+            rate = ins / (stage[k]["ms_per_launch"] / 1000.0)
+            peak_rate = props.multi_processor_count * 4 * (clocks["sm_mhz"] or clocks["sm_max_mhz"] or 0) * 1e6
+            onchip[k] = {"bound": "issue", "achieved": rate / 1e12, "peak": peak_rate / 1e12,
+                         "unit": "T warp-instr/s", "frac": rate / peak_rate if peak_rate else None,
+                         "warp_instructions_per_launch": ins,
+                         "ncu_lsu_data_pipe_pct": traffic[k].get("lsu_data_pipe_pct")}
+    roofline["onchip"] = onchip
 
     # end to end through the public API with host buffers: load (host->device of the
     # sinogram and normalization) + 32 sub-iterations + scaled image back to the host
