@@ -13,6 +13,9 @@
 //   --subsets S  --iterations N  --write-every K  --device D
 //   --vlor-endpoints   the VLOR file holds two LORs of float32 endpoints per
 //                      event (gf_read_vlor_endpoints) instead of int32 bins
+//   --storage f32|f16|bf16   element type of the per-subset ratio sinogram
+//                            (arithmetic stays FP32; default f32)
+//   --tune             pick the projectors' tile shapes by timing first
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -28,7 +31,7 @@ static int usage() {
   printf("3 Inputs --> Reconstruction Doubles & Triples [Input = Sinog_Doubles + Sinog_Triples + Sinog_Normalization] \n");
   printf("4 Inputs --> VLOR reconstruction [Input = Sinog_Doubles + Sinog_Triples + Sinog_Normalization + Vlor_file] \n");
   printf("options: --geometry res,nzs,nrad,nang,span,nseg,pitch,diam,fov --subsets S --iterations N "
-         "--write-every K --device D --vlor-endpoints\n");
+         "--write-every K --device D --vlor-endpoints --storage f32|f16|bf16 --tune\n");
   return 0;
 }
 
@@ -41,7 +44,8 @@ int main(int argc, char** argv) {
   gf_geometry g;
   gf_geometry_reference(&g);
   int nsub = 1, niter = -1, every = 20, device = 0;
-  bool vlor_endpoints = false;
+  bool vlor_endpoints = false, tune = false;
+  int storage = GF_STORE_F32;
   std::vector<std::string> files;
   for (int i = 1; i < argc; i++) {
     std::string a = argv[i];
@@ -69,6 +73,17 @@ int main(int argc, char** argv) {
       device = atoi(val("--device"));
     } else if (a == "--vlor-endpoints") {
       vlor_endpoints = true;
+    } else if (a == "--tune") {
+      tune = true;
+    } else if (a == "--storage") {
+      const std::string v = val("--storage");
+      if (v == "f32") storage = GF_STORE_F32;
+      else if (v == "f16") storage = GF_STORE_F16;
+      else if (v == "bf16") storage = GF_STORE_BF16;
+      else {
+        fprintf(stderr, "gfirst: --storage wants f32, f16 or bf16\n");
+        return 2;
+      }
     } else if (a == "-h" || a == "--help") {
       return usage();
     } else {
@@ -85,6 +100,12 @@ int main(int argc, char** argv) {
   gf_recon_params p;
   gf_recon_defaults(mode, &p);
   if (niter >= 0) p.niter = niter;
+  p.storage = storage;
+  if (tune) {
+    int32_t R, chunk, warps;
+    if ((st = gf_tune(ctx, &R, &chunk, &warps)) != GF_OK) return die("gf_tune", st);
+    printf("Tile shapes: R %d, %d steps per chunk, %d back-projector warps\n", R, chunk, warps);
+  }
   gf_recon* r = nullptr;
   if ((st = gf_recon_create(ctx, &p, &r)) != GF_OK) return die("gf_recon_create", st);
   printf("Starting............ \n");

@@ -324,6 +324,26 @@ def test_cli_end_to_end_matches_reference(gf, tmp_path):
     assert rel(ld("SINOG_VLOR.raw"), z["m3_sinog_vlor"]) < IMG_TOL
 
 
+def test_cli_storage_and_tune_options(gf, tmp_path):
+    """`--tune` keeps the results; `--storage bf16` stays close to FP32 (mode 1)."""
+    name = "tinyb"
+    geo = case(name)
+    for k, v in inputs.case_files(name).items():
+        (tmp_path / k).write_bytes(v)
+    gs = ",".join(str(x) for x in geo)
+    imgs = {}
+    for tag, extra in (("plain", []), ("tuned", ["--tune"]), ("bf16", ["--storage", "bf16"])):
+        d = tmp_path / tag
+        d.mkdir()
+        cmd = [str(gf.CLI_PATH), "--geometry", gs, "--subsets", "3", "--iterations", "20", *extra,
+               str(tmp_path / "sinoD.raw"), str(tmp_path / "norm.raw")]
+        out = subprocess.run(cmd, cwd=d, capture_output=True, text=True)
+        assert out.returncode == 0, out.stderr
+        imgs[tag] = np.fromfile(d / "img_GPU_D_ITER20.raw", np.float32)
+    assert rel(imgs["tuned"], imgs["plain"]) < 1e-6
+    assert rel(imgs["bf16"], imgs["plain"]) < 1e-2
+
+
 # ---------------------------------------------------------------- full preclinical size
 @pytest.fixture(scope="module")
 def c2(gf):
