@@ -800,7 +800,23 @@ def run_triples(args) -> int:
         dt = time.perf_counter() - t0
         imgs[storage] = (r.image(0), r.image(1))
         out[storage] = {"seconds": dt, "subiters_per_s": 2 * nsub * niter / dt}
+        # stage times of the same reconstruction (library CUDA events), not timed above
+        r.restart()
+        r.profile(True)
+        r.iterate(niter)
+        stages = {}
+        for name, sid in gf.STAGES.items():
+            tot, n = r.profile_read(sid)
+            if n:
+                stages[name] = {"launches": n, "ms_per_launch": tot / n, "total_ms": tot}
+        out[storage]["stages"] = stages
+        r.profile(False)
         r.close()
+    if not args.fp64_oracle:
+        print(json.dumps({"workload": "triples", "arms": out, "config": {"events": nev, "subsets": nsub,
+                                                                         "iterations": niter}}))
+        ctx.close()
+        return 0
     # FP64 oracle on the host (the checker)
     sys.path.insert(0, str(ROOT / "oracle"))
     import gfo
@@ -963,6 +979,7 @@ def main() -> int:
     ap.add_argument("--workload", default="recon", choices=["recon", "frames", "serving", "triples", "small", "cli"])
     ap.add_argument("--events", type=int, default=2_000_000)
     ap.add_argument("--fp32-oracle", type=int, default=1, help="triples: also compare with the FP32 oracle")
+    ap.add_argument("--fp64-oracle", type=int, default=1, help="triples: compare with the FP64 oracle (0: GPU only)")
     ap.add_argument("--frames", type=int, default=32)
     ap.add_argument("--frames-geometry", default="preclinical", choices=["preclinical", "small"])
     ap.add_argument("--serve-rate", type=float, default=20.0)
