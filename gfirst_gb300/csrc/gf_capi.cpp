@@ -492,7 +492,27 @@ gf_status gf_vlor_count(gf_ctx* c, const int32_t* d_ev, int64_t n, float* d_coun
 gf_status gf_vlor_split(gf_ctx* c, const int32_t* d_ev, int64_t n, const float* d_proj, const float* d_blankt,
                         float* d_out) {
   if (!c || (!d_ev && n) || !d_proj || !d_blankt || !d_out || n < 0) return set_error(GF_ERR_ARG, "bad argument");
-  GF_LAUNCH(c, launch_vlor_split(c->dg, d_ev, n, d_proj, d_blankt, d_out, c->stream));
+  if (n == 0) return GF_OK;
+  if (n >= (1ll << 30)) return set_error(GF_ERR_ARG, "more than 2^30 events");
+  // event ends sorted by (bin, event) in temporaries, then every bin's shares
+  // added in event order: the reference's sums, no atomics
+  cudaStream_t st = c->stream;
+  unsigned long long *keys_tmp = nullptr, *keys = nullptr;
+  void* temp = nullptr;
+  const size_t tb = vlor_sort_temp_bytes(n);
+  cudaError_t e = cudaMallocAsync(&keys_tmp, (size_t)n * 2 * sizeof(unsigned long long), st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&keys, (size_t)n * 2 * sizeof(unsigned long long), st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&temp, tb ? tb : 16, st);
+  if (e == cudaSuccess) e = launch_vlor_sort(c->dg, d_ev, n, keys_tmp, keys, temp, tb, st);
+  if (e == cudaSuccess) e = launch_vlor_split_sorted(keys, n, d_ev, d_proj, d_blankt, d_out, st);
+  if (e == cudaSuccess) c->launches += 3;
+  if (keys_tmp) cudaFreeAsync(keys_tmp, st);
+  if (keys) cudaFreeAsync(keys, st);
+  if (temp) cudaFreeAsync(temp, st);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_error(e, "VLOR split");
+  }
   return GF_OK;
 }
 

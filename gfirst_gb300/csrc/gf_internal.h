@@ -98,7 +98,8 @@ struct gf_recon {
   bool cyl_proj_ready = false;  // proj_ref holds the unit-cylinder projection (modes 1-3)
   float* proj_t = nullptr;  // triples projection, file layout (VLOR split weights)
   int32_t* events = nullptr;
-  int64_t nev = 0;
+  unsigned long long* vlor_keys = nullptr;  // event ends sorted by (bin, event), 2*nev
+  int64_t nev = 0, ev_cap = 0;
   float* blankt = nullptr;
   float* datos_v = nullptr;
   float* d_max = nullptr;

@@ -93,7 +93,7 @@ gf_status gf_recon::subiteration(int t, int s) {
     stage_end();
     stage_begin(GF_STAGE_VLOR);
     GF_CK(cudaMemsetAsync(datos_v, 0, (size_t)pl.ndata * sizeof(float), st));
-    GF_LAUNCH(c, launch_vlor_split(c->dg, events, nev, proj_t, blankt, datos_v, st));
+    GF_LAUNCH(c, launch_vlor_split_sorted(vlor_keys, nev, events, proj_t, blankt, datos_v, st));
     GF_LAUNCH(c, launch_ratio_gather(c->dg, c->d_rowmap, s, na, proj_t, datos_v, dbg[1] + off, cal + off, corrcal,
                                      p.storage, st));
     stage_end();
@@ -254,8 +254,22 @@ static gf_status load_impl(gf_recon* r, const float* h_image, const float* h_dsi
   if (mode == 3) {
     r->nev = nevents;
     if (nevents > 0) {
-      if ((s = r->alloc_t((size_t)nevents * 2, &r->events)) != GF_OK) return done(s);
+      if (nevents > r->ev_cap) {
+        if ((s = r->alloc_t((size_t)nevents * 2, &r->events)) != GF_OK) return done(s);
+        if ((s = r->alloc_t((size_t)nevents * 2, &r->vlor_keys)) != GF_OK) return done(s);
+        r->ev_cap = nevents;
+      }
       if ((s = ck(cudaMemcpyAsync(r->events, h_events, (size_t)nevents * 2 * sizeof(int32_t), cudaMemcpyHostToDevice, st), "upload events")) != GF_OK) return done(s);
+      // the event ends in the order the VLOR split adds them (temporaries stream-ordered)
+      unsigned long long* keys_tmp = nullptr;
+      void* temp = nullptr;
+      const size_t tb = vlor_sort_temp_bytes(nevents);
+      cudaError_t e = cudaMallocAsync(&keys_tmp, (size_t)nevents * 2 * sizeof(unsigned long long), st);
+      if (e == cudaSuccess) e = cudaMallocAsync(&temp, tb ? tb : 16, st);
+      if (e == cudaSuccess) e = launch_vlor_sort(c->dg, r->events, nevents, keys_tmp, r->vlor_keys, temp, tb, st);
+      if (keys_tmp) cudaFreeAsync(keys_tmp, st);
+      if (temp) cudaFreeAsync(temp, st);
+      if ((s = ck(e, "sort VLOR events")) != GF_OK) return done(s);
     }
     // counts in datos_v (scratch for now), then BLANKT (GFIRST.cu:229-247)
     if ((s = ck(cudaMemsetAsync(r->datos_v, 0, pl.ndata * sizeof(float), st), "memset")) != GF_OK) return done(s);

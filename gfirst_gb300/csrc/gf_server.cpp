@@ -13,8 +13,7 @@
 // the running ones.  A finished request's image is read back, its memory
 // returned (stream-ordered, to the device's pool), and the loader
 // re-examines the queue.  Results do not depend on what else runs: each
-// request owns its buffers and the kernels are deterministic for modes 0
-// and 1.
+// request owns its buffers and the kernels are deterministic.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -232,7 +231,7 @@ gf_status gf_recon_bytes(const gf_geometry* gg, int32_t nsub, const gf_recon_par
     b += 3 * d;                                                                   // staging
   }
   if (p->mode >= 2) b += all * 8 + v;
-  if (p->mode == 3) b += 3 * d + nev * 8;
+  if (p->mode == 3) b += 3 * d + nev * (8 + 16);  // events and their sorted ends
   *bytes = b;
   return GF_OK;
 }

@@ -5,6 +5,8 @@
 // Elements of a subset-layout array are indexed by
 //   (angle-in-subset tl, radial bin r, padded row p): (tl*NRAD + r)*PS + p,
 // with one array holding every subset back to back when it is static.
+#include <cub/device/device_radix_sort.cuh>
+
 #include "gf_kernels.h"
 
 namespace gf {
@@ -245,25 +247,70 @@ cudaError_t launch_blankt(const DevGeom& g, const float* cnt, const float* tsino
   return cudaGetLastError();
 }
 
-__global__ void vlor_split_kernel(const int32_t* __restrict__ ev, long long nev, long long ndata,
-                                  const float* __restrict__ proj, const float* __restrict__ bl, float* out) {
+// ---- VLOR split in the reference's order ------------------------------------
+// The reference adds each event's two shares to their bins in file order
+// (GFIRST.cu:373-389), so a bin's sum is its shares added in event order.
+// One 64-bit key per event end, (bin << 32) | (2*event + end), sorted once,
+// puts each bin's shares in that order; the split then sums each bin's run
+// sequentially: the same additions in the same order, without atomics.
+constexpr unsigned long long kNoKey = ~0ull;  // an end of a rejected event
+
+__global__ void vlor_keys_kernel(const int32_t* __restrict__ ev, long long nev, long long ndata,
+                                 unsigned long long* keys) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nev) return;
   long long i1, i2;
-  if (!vlor_bins(ev, e, ndata, &i1, &i2)) return;
-  const float valor = __fadd_rn(bl[i1], bl[i2]);
-  const float s1 = proj[i1], s2 = proj[i2];
-  const float s = __fadd_rn(s1, s2);
-  const float s_inv = (s > 0.01f) ? (float)__drcp_rn((double)s) : 0.f;
-  atomicAdd(out + i1, __fmul_rn(__fmul_rn(s1, s_inv), valor));
-  atomicAdd(out + i2, __fmul_rn(__fmul_rn(s2, s_inv), valor));
+  const bool ok = vlor_bins(ev, e, ndata, &i1, &i2);
+  keys[2 * e] = ok ? ((unsigned long long)i1 << 32) | (unsigned long long)(2 * e) : kNoKey;
+  keys[2 * e + 1] = ok ? ((unsigned long long)i2 << 32) | (unsigned long long)(2 * e + 1) : kNoKey;
 }
 
-cudaError_t launch_vlor_split(const DevGeom& g, const int32_t* ev, long long nev, const float* proj,
-                              const float* blankt, float* out, cudaStream_t st) {
+size_t vlor_sort_temp_bytes(long long nev) {
+  size_t bytes = 0;
+  cub::DeviceRadixSort::SortKeys(nullptr, bytes, (const unsigned long long*)nullptr,
+                                 (unsigned long long*)nullptr, (int)(2 * nev), 0, 64);
+  return bytes;
+}
+
+cudaError_t launch_vlor_sort(const DevGeom& g, const int32_t* ev, long long nev, unsigned long long* keys_tmp,
+                             unsigned long long* keys, void* temp, size_t temp_bytes, cudaStream_t st) {
   if (nev <= 0) return cudaSuccess;
+  if (nev >= (1ll << 30)) return cudaErrorInvalidValue;  // 2*event + end must fit 32 bits, counts an int
   const long long ndata = (long long)g.P * g.nang * g.nrad;
-  vlor_split_kernel<<<(unsigned)((nev + 255) / 256), 256, 0, st>>>(ev, nev, ndata, proj, blankt, out);
+  vlor_keys_kernel<<<(unsigned)((nev + 255) / 256), 256, 0, st>>>(ev, nev, ndata, keys_tmp);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return cub::DeviceRadixSort::SortKeys(temp, temp_bytes, keys_tmp, keys, (int)(2 * nev), 0, 64, st);
+}
+
+__global__ void vlor_split_sorted_kernel(const unsigned long long* __restrict__ keys, long long n,
+                                         const int32_t* __restrict__ ev, const float* __restrict__ proj,
+                                         const float* __restrict__ bl, float* out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long k = keys[i];
+  if (k == kNoKey) return;
+  const unsigned long long bin = k >> 32;
+  if (i > 0 && (keys[i - 1] >> 32) == bin) return;  // not the first share of its bin
+  float sum = out[bin];  // the shares are added to out, as the reference adds them to SINOG_VLOR
+  for (long long j = i; j < n && (keys[j] >> 32) == bin; j++) {
+    const long long ie = (long long)(keys[j] & 0xffffffffull);
+    const long long e = ie >> 1;
+    const long long i1 = (long long)ev[2 * e] - 1, i2 = (long long)ev[2 * e + 1] - 1;
+    const float valor = __fadd_rn(bl[i1], bl[i2]);
+    const float s1 = proj[i1], s2 = proj[i2];
+    const float s = __fadd_rn(s1, s2);
+    const float s_inv = (s > 0.01f) ? (float)__drcp_rn((double)s) : 0.f;
+    sum = __fadd_rn(sum, __fmul_rn(__fmul_rn((ie & 1) ? s2 : s1, s_inv), valor));
+  }
+  out[bin] = sum;
+}
+
+cudaError_t launch_vlor_split_sorted(const unsigned long long* keys, long long nev, const int32_t* ev,
+                                     const float* proj, const float* blankt, float* out, cudaStream_t st) {
+  if (nev <= 0) return cudaSuccess;
+  const long long n = 2 * nev;
+  vlor_split_sorted_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(keys, n, ev, proj, blankt, out);
   return cudaGetLastError();
 }
 

@@ -125,8 +125,11 @@ gf_status gf_bilateral(gf_ctx* ctx, const float* d_in, const float* d_ref, float
 /* VLOR end counts (d_count must be zeroed by the caller), GFIRST.cu:229-240.
  * Events are int32 pairs of 1-based bins. */
 gf_status gf_vlor_count(gf_ctx* ctx, const int32_t* d_events, int64_t nevents, float* d_count);
-/* VLOR split of each event between its two bins in proportion to d_proj
- * (d_out must be zeroed by the caller), GFIRST.cu:373-389. */
+/* VLOR split of each event between its two bins in proportion to d_proj,
+ * added to d_out (zeroed by the caller for the reference's SINOG_VLOR),
+ * GFIRST.cu:373-389.  Each bin's shares are added in event order, as the
+ * reference's loop adds them, so the result is the reference's bit for bit;
+ * the ordering uses device temporaries of 32 bytes per event. */
 gf_status gf_vlor_split(gf_ctx* ctx, const int32_t* d_events, int64_t nevents, const float* d_proj,
                         const float* d_blankt, float* d_out);
 
