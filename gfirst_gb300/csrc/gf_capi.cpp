@@ -498,16 +498,19 @@ gf_status gf_vlor_split(gf_ctx* c, const int32_t* d_ev, int64_t n, const float* 
   // added in event order: the reference's sums, no atomics
   cudaStream_t st = c->stream;
   unsigned long long *keys_tmp = nullptr, *keys = nullptr;
+  float* share = nullptr;
   void* temp = nullptr;
   const size_t tb = vlor_sort_temp_bytes(n);
   cudaError_t e = cudaMallocAsync(&keys_tmp, (size_t)n * 2 * sizeof(unsigned long long), st);
   if (e == cudaSuccess) e = cudaMallocAsync(&keys, (size_t)n * 2 * sizeof(unsigned long long), st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&share, (size_t)n * 2 * sizeof(float), st);
   if (e == cudaSuccess) e = cudaMallocAsync(&temp, tb ? tb : 16, st);
   if (e == cudaSuccess) e = launch_vlor_sort(c->dg, d_ev, n, keys_tmp, keys, temp, tb, st);
-  if (e == cudaSuccess) e = launch_vlor_split_sorted(keys, n, d_ev, d_proj, d_blankt, d_out, st);
-  if (e == cudaSuccess) c->launches += 3;
+  if (e == cudaSuccess) e = launch_vlor_split_sorted(c->dg, keys, n, d_ev, d_proj, d_blankt, share, d_out, st);
+  if (e == cudaSuccess) c->launches += 4;
   if (keys_tmp) cudaFreeAsync(keys_tmp, st);
   if (keys) cudaFreeAsync(keys, st);
+  if (share) cudaFreeAsync(share, st);
   if (temp) cudaFreeAsync(temp, st);
   if (e != cudaSuccess) {
     cudaGetLastError();

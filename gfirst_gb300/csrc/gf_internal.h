@@ -99,6 +99,7 @@ struct gf_recon {
   float* proj_t = nullptr;  // triples projection, file layout (VLOR split weights)
   int32_t* events = nullptr;
   unsigned long long* vlor_keys = nullptr;  // event ends sorted by (bin, event), 2*nev
+  float* vlor_share = nullptr;              // each event end's share of one split, 2*nev
   int64_t nev = 0, ev_cap = 0;
   float* blankt = nullptr;
   float* datos_v = nullptr;

@@ -97,12 +97,14 @@ cudaError_t launch_blankt(const DevGeom& g, const float* cnt, const float* tsino
 
 // The split in the reference's order: keys of the event ends sorted by (bin,
 // event) once (launch_vlor_sort; keys_tmp and keys hold 2*nev entries, temp
-// vlor_sort_temp_bytes(nev) bytes), then each bin's shares summed in order.
+// vlor_sort_temp_bytes(nev) bytes), then each event's two shares computed into
+// share (2*nev floats) and each bin's shares summed in event order.
 size_t vlor_sort_temp_bytes(long long nev);
 cudaError_t launch_vlor_sort(const DevGeom& g, const int32_t* ev, long long nev, unsigned long long* keys_tmp,
                              unsigned long long* keys, void* temp, size_t temp_bytes, cudaStream_t st);
-cudaError_t launch_vlor_split_sorted(const unsigned long long* keys, long long nev, const int32_t* ev,
-                                     const float* proj, const float* blankt, float* out, cudaStream_t st);
+cudaError_t launch_vlor_split_sorted(const DevGeom& g, const unsigned long long* keys, long long nev,
+                                     const int32_t* ev, const float* proj, const float* blankt, float* share,
+                                     float* out, cudaStream_t st);
 
 cudaError_t launch_vlor_endpoints(const DevGeom& g, const float* lors, long long n, float vx, float hs, int32_t* ev,
                                   cudaStream_t st);

@@ -93,7 +93,7 @@ gf_status gf_recon::subiteration(int t, int s) {
     stage_end();
     stage_begin(GF_STAGE_VLOR);
     GF_CK(cudaMemsetAsync(datos_v, 0, (size_t)pl.ndata * sizeof(float), st));
-    GF_LAUNCH(c, launch_vlor_split_sorted(vlor_keys, nev, events, proj_t, blankt, datos_v, st));
+    GF_LAUNCH(c, launch_vlor_split_sorted(c->dg, vlor_keys, nev, events, proj_t, blankt, vlor_share, datos_v, st));
     GF_LAUNCH(c, launch_ratio_gather(c->dg, c->d_rowmap, s, na, proj_t, datos_v, dbg[1] + off, cal + off, corrcal,
                                      p.storage, st));
     stage_end();
@@ -257,6 +257,7 @@ static gf_status load_impl(gf_recon* r, const float* h_image, const float* h_dsi
       if (nevents > r->ev_cap) {
         if ((s = r->alloc_t((size_t)nevents * 2, &r->events)) != GF_OK) return done(s);
         if ((s = r->alloc_t((size_t)nevents * 2, &r->vlor_keys)) != GF_OK) return done(s);
+        if ((s = r->alloc_t((size_t)nevents * 2, &r->vlor_share)) != GF_OK) return done(s);
         r->ev_cap = nevents;
       }
       if ((s = ck(cudaMemcpyAsync(r->events, h_events, (size_t)nevents * 2 * sizeof(int32_t), cudaMemcpyHostToDevice, st), "upload events")) != GF_OK) return done(s);

@@ -231,7 +231,7 @@ gf_status gf_recon_bytes(const gf_geometry* gg, int32_t nsub, const gf_recon_par
     b += 3 * d;                                                                   // staging
   }
   if (p->mode >= 2) b += all * 8 + v;
-  if (p->mode == 3) b += 3 * d + nev * (8 + 16);  // events and their sorted ends
+  if (p->mode == 3) b += 3 * d + nev * (8 + 16 + 8);  // events, their sorted ends, their shares
   *bytes = b;
   return GF_OK;
 }

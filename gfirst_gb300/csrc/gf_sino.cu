@@ -283,9 +283,25 @@ cudaError_t launch_vlor_sort(const DevGeom& g, const int32_t* ev, long long nev,
   return cub::DeviceRadixSort::SortKeys(temp, temp_bytes, keys_tmp, keys, (int)(2 * nev), 0, 64, st);
 }
 
+// pass 1, over events: both shares of each event, share[2e + end]
+__global__ void vlor_shares_kernel(const int32_t* __restrict__ ev, long long nev, long long ndata,
+                                   const float* __restrict__ proj, const float* __restrict__ bl, float* share) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nev) return;
+  long long i1, i2;
+  if (!vlor_bins(ev, e, ndata, &i1, &i2)) return;  // its keys are kNoKey: never read
+  const float valor = __fadd_rn(bl[i1], bl[i2]);
+  const float s1 = proj[i1], s2 = proj[i2];
+  const float s = __fadd_rn(s1, s2);
+  const float s_inv = (s > 0.01f) ? (float)__drcp_rn((double)s) : 0.f;
+  share[2 * e] = __fmul_rn(__fmul_rn(s1, s_inv), valor);
+  share[2 * e + 1] = __fmul_rn(__fmul_rn(s2, s_inv), valor);
+}
+
+// pass 2, over the sorted ends: the first end of each bin adds the bin's
+// shares in event order
 __global__ void vlor_split_sorted_kernel(const unsigned long long* __restrict__ keys, long long n,
-                                         const int32_t* __restrict__ ev, const float* __restrict__ proj,
-                                         const float* __restrict__ bl, float* out) {
+                                         const float* __restrict__ share, float* out) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const unsigned long long k = keys[i];
@@ -293,24 +309,20 @@ __global__ void vlor_split_sorted_kernel(const unsigned long long* __restrict__ 
   const unsigned long long bin = k >> 32;
   if (i > 0 && (keys[i - 1] >> 32) == bin) return;  // not the first share of its bin
   float sum = out[bin];  // the shares are added to out, as the reference adds them to SINOG_VLOR
-  for (long long j = i; j < n && (keys[j] >> 32) == bin; j++) {
-    const long long ie = (long long)(keys[j] & 0xffffffffull);
-    const long long e = ie >> 1;
-    const long long i1 = (long long)ev[2 * e] - 1, i2 = (long long)ev[2 * e + 1] - 1;
-    const float valor = __fadd_rn(bl[i1], bl[i2]);
-    const float s1 = proj[i1], s2 = proj[i2];
-    const float s = __fadd_rn(s1, s2);
-    const float s_inv = (s > 0.01f) ? (float)__drcp_rn((double)s) : 0.f;
-    sum = __fadd_rn(sum, __fmul_rn(__fmul_rn((ie & 1) ? s2 : s1, s_inv), valor));
-  }
+  for (long long j = i; j < n && (keys[j] >> 32) == bin; j++) sum = __fadd_rn(sum, share[keys[j] & 0xffffffffull]);
   out[bin] = sum;
 }
 
-cudaError_t launch_vlor_split_sorted(const unsigned long long* keys, long long nev, const int32_t* ev,
-                                     const float* proj, const float* blankt, float* out, cudaStream_t st) {
+cudaError_t launch_vlor_split_sorted(const DevGeom& g, const unsigned long long* keys, long long nev,
+                                     const int32_t* ev, const float* proj, const float* blankt, float* share,
+                                     float* out, cudaStream_t st) {
   if (nev <= 0) return cudaSuccess;
+  const long long ndata = (long long)g.P * g.nang * g.nrad;
+  vlor_shares_kernel<<<(unsigned)((nev + 255) / 256), 256, 0, st>>>(ev, nev, ndata, proj, blankt, share);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
   const long long n = 2 * nev;
-  vlor_split_sorted_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(keys, n, ev, proj, blankt, out);
+  vlor_split_sorted_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(keys, n, share, out);
   return cudaGetLastError();
 }
 

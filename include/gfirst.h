@@ -129,7 +129,7 @@ gf_status gf_vlor_count(gf_ctx* ctx, const int32_t* d_events, int64_t nevents, f
  * added to d_out (zeroed by the caller for the reference's SINOG_VLOR),
  * GFIRST.cu:373-389.  Each bin's shares are added in event order, as the
  * reference's loop adds them, so the result is the reference's bit for bit;
- * the ordering uses device temporaries of 32 bytes per event. */
+ * the ordering uses device temporaries of 40 bytes per event. */
 gf_status gf_vlor_split(gf_ctx* ctx, const int32_t* d_events, int64_t nevents, const float* d_proj,
                         const float* d_blankt, float* d_out);
 
