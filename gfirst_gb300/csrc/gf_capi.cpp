@@ -202,11 +202,9 @@ gf_status gf_create(const gf_geometry* g, int32_t nsubsets, int32_t device, gf_c
   if (!(prop.major == 10 && prop.minor == 3))
     return set_error(GF_ERR_NODEV, std::string("this library is built for sm_103a; device is ") + prop.name);
   FpSchedule fps;
-  int R = fp_default_R(plan);
-  if (const char* v = getenv("GF_FP_R")) R = atoi(v);
-  int lc = 32;
-  if (const char* v = getenv("GF_FP_LC")) lc = atoi(v);
-  if (!make_fp_schedule(plan, R, lc, &fps)) return set_error(GF_ERR_GEOMETRY, "no forward-projector schedule fits");
+  // default tile shapes; gf_tune picks them by timing
+  if (!make_fp_schedule(plan, fp_default_R(plan), 32, &fps))
+    return set_error(GF_ERR_GEOMETRY, "no forward-projector schedule fits");
 
   {
     // keep memory returned by cudaFreeAsync cached in the device's pool, so
