@@ -642,6 +642,21 @@ def run_small(args) -> int:
     ctx.sync()
     dt = (time.perf_counter() - t0) / steps
     gpu_img = r.image(0)
+    # the same reconstruction with the image and the ratio sinogram in FP16
+    r16 = gf.Recon(ctx, 1, niter=niter, storage="f16", image_storage="f16")
+    r16.load(dsino=dsino, norm=norm)
+    for _ in range(args.warmup):
+        r16.restart()
+        r16.iterate(niter)
+    ctx.sync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        r16.restart()
+        r16.iterate(niter)
+    ctx.sync()
+    dt16 = (time.perf_counter() - t0) / steps
+    img16 = r16.image(0)
+    r16.close()
     # end to end: load from host buffers, iterate, read the image back
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -679,6 +694,8 @@ def run_small(args) -> int:
                              "seconds": cpu_s},
             "gpu_vs_cpu_speedup": (subiters / dt) / (subiters / cpu_s),
             "rel_l2_vs_fp32_oracle": rel(gpu_img, ref32["img_d"]), "rel_l2_vs_fp64_oracle": rel(gpu_img, ref64["img_d"]),
+            "fp16_image_and_ratio": {"subiters_per_s": subiters / dt16, "ms_per_step": 1000.0 * dt16,
+                                     "rel_l2_vs_fp64_oracle": rel(img16, ref64["img_d"])},
             "fp32_oracle_vs_fp64": rel(ref32["img_d"], ref64["img_d"])}
     print(json.dumps(line))
     return 0

@@ -37,7 +37,7 @@ class _CGeom(ctypes.Structure):
 class _CParams(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("niter", ctypes.c_int32), ("psf_fw", ctypes.c_float),
                 ("psf_bw", ctypes.c_float), ("scale_d", ctypes.c_float), ("scale_t", ctypes.c_float),
-                ("storage", ctypes.c_int32)]
+                ("storage", ctypes.c_int32), ("image_storage", ctypes.c_int32)]
 
 
 STORE = {"f32": 0, "f16": 1, "bf16": 2}
@@ -267,10 +267,11 @@ class Recon:
     """gf_recon: one reconstruction of a CLI mode, resident on the device."""
 
     def __init__(self, ctx: Context, mode: int, niter: int = 60, psf_fw: float = 1.5, psf_bw: float = 1.5,
-                 storage: str = "f32"):
+                 storage: str = "f32", image_storage: str = "f32"):
         self.ctx, self.mode = ctx, mode
         p = recon_defaults(mode)
         p.niter, p.psf_fw, p.psf_bw, p.storage = niter, psf_fw, psf_bw, STORE[storage]
+        p.image_storage = STORE[image_storage]
         self.params = p
         h = ctypes.c_void_p()
         _ck(lib().gf_recon_create(ctx.h, ctypes.byref(p), ctypes.byref(h)))

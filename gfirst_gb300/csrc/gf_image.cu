@@ -10,13 +10,22 @@
 
 namespace gf {
 
+// Image elements: FP32, or FP16/BF16 storage of the doubles image in mode 1
+// (every operation in FP32; a store rounds to nearest even).
+__device__ __forceinline__ float img_ld(const float* p) { return *p; }
+__device__ __forceinline__ float img_ld(const __half* p) { return __half2float(*p); }
+__device__ __forceinline__ float img_ld(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+__device__ __forceinline__ void img_st(float* p, float v) { *p = v; }
+__device__ __forceinline__ void img_st(__half* p, float v) { *p = __float2half_rn(v); }
+__device__ __forceinline__ void img_st(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+
 // ---- separable XY Gaussian, GFIRST_GPU_Kernels.cu:332-358 -----------------
 // CTA: 8x8 columns x 32 slices.  The y pass is zero-padded; the x pass runs
 // only for 3 < x < RES-4 and border columns output the raw input.  With DIV
 // the input is the update ratio numer/denom (1 where denom < 0.001,
 // divVxVGPU, GFIRST_GPU_Kernels.cu:173-182), computed on the fly.
-template <bool DIV>
-__global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const float* __restrict__ in,
+template <bool DIV, class T>
+__global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const T* __restrict__ in,
                                                       const float* __restrict__ den, const Taps9 G,
                                                       float* __restrict__ out) {
   __shared__ float S[16][16][32];
@@ -29,7 +38,7 @@ __global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const flo
     for (int c = ty; c < 256; c += 8) {
       const int yy = c >> 4, xx = c & 15;
       const int y = y0 - 4 + yy, x = x0 - 4 + xx;
-      S[yy][xx][lane] = (y >= 0 && y < RES && x >= 0 && x < RES) ? in[((size_t)y * RES + x) * NZP + z] : 0.f;
+      S[yy][xx][lane] = (y >= 0 && y < RES && x >= 0 && x < RES) ? img_ld(in + ((size_t)y * RES + x) * NZP + z) : 0.f;
     }
   }
   // with DIV, batches of eight columns: every load of a batch is issued before
@@ -47,7 +56,7 @@ __global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const flo
       const int y = y0 - 4 + (c >> 4), x = x0 - 4 + (c & 15);
       ok[u] = y >= 0 && y < RES && x >= 0 && x < RES;
       o[u] = ok[u] ? ((size_t)y * RES + x) * NZP + z : 0;
-      nv[u] = ok[u] ? in[o[u]] : 0.f;
+      nv[u] = ok[u] ? img_ld(in + o[u]) : 0.f;
       if (DIV) dv[u] = ok[u] ? den[o[u]] : 1.f;
     }
 #pragma unroll
@@ -85,11 +94,20 @@ __global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const flo
   }
 }
 
-cudaError_t launch_conv_xy(const DevGeom& g, const float* in, const float* den, const Taps9& t, float* out,
-                           cudaStream_t st) {
+cudaError_t launch_conv_xy(const DevGeom& g, const void* in, const float* den, const Taps9& t, float* out,
+                           cudaStream_t st, int in_store) {
   dim3 grid((g.res + 7) / 8, (g.res + 7) / 8, g.nzp / 32);
-  if (den) conv_xy_kernel<true><<<grid, 256, 0, st>>>(g, in, den, t, out);
-  else conv_xy_kernel<false><<<grid, 256, 0, st>>>(g, in, nullptr, t, out);
+  if (den) {
+    if (in_store != 0) return cudaErrorInvalidValue;
+    conv_xy_kernel<true, float><<<grid, 256, 0, st>>>(g, static_cast<const float*>(in), den, t, out);
+  } else if (in_store == 1) {
+    conv_xy_kernel<false, __half><<<grid, 256, 0, st>>>(g, static_cast<const __half*>(in), nullptr, t, out);
+  } else if (in_store == 2) {
+    conv_xy_kernel<false, __nv_bfloat16><<<grid, 256, 0, st>>>(g, static_cast<const __nv_bfloat16*>(in), nullptr, t,
+                                                                out);
+  } else {
+    conv_xy_kernel<false, float><<<grid, 256, 0, st>>>(g, static_cast<const float*>(in), nullptr, t, out);
+  }
   return cudaGetLastError();
 }
 
@@ -118,9 +136,9 @@ __device__ __forceinline__ float zrule(const float* c, int ze, int K, int NZS, c
 // values as the reference's multiply-then-copy order requires.  Voxel 0's
 // factor (DENOM[0] in the reference) only reaches slice 0, which the edge
 // copy overwrites.
-template <int Q>
+template <int Q, class T>
 __global__ void __launch_bounds__(256) zfilter_update_kernel(const DevGeom g, const float* __restrict__ C,
-                                                             const Taps5 t5, float* img) {
+                                                             const Taps5 t5, T* img) {
   const int lane = threadIdx.x & 31;
   const int colidx = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (colidx >= g.res * g.res) return;  // whole warp
@@ -128,7 +146,7 @@ __global__ void __launch_bounds__(256) zfilter_update_kernel(const DevGeom g, co
   const int NZS = g.nzs;
   float v[Q];
 #pragma unroll
-  for (int q = 0; q < Q; q++) v[q] = img[cb + lane + 32 * q];
+  for (int q = 0; q < Q; q++) v[q] = img_ld(img + cb + lane + 32 * q);
   const float s1 = __shfl_sync(0xffffffffu, v[0], 1);
   float sl = 0.f;
 #pragma unroll
@@ -146,24 +164,31 @@ __global__ void __launch_bounds__(256) zfilter_update_kernel(const DevGeom g, co
       const int K = (colidx == 0) ? ze - 1 : ze;
       out = __fmul_rn(iv, zrule(C + cb, ze, K, NZS, t5));
     }
-    img[cb + z] = out;
+    img_st(img + cb + z, out);
   }
 }
 
-cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const Taps5& t5, float* img, cudaStream_t st) {
+template <class T>
+static cudaError_t zfilter_update_t(const DevGeom& g, const float* C, const Taps5& t5, T* img, cudaStream_t st) {
   dim3 grid((g.res * g.res + 7) / 8);
   switch (g.nzp / 32) {
-    case 1: zfilter_update_kernel<1><<<grid, 256, 0, st>>>(g, C, t5, img); break;
-    case 2: zfilter_update_kernel<2><<<grid, 256, 0, st>>>(g, C, t5, img); break;
-    case 3: zfilter_update_kernel<3><<<grid, 256, 0, st>>>(g, C, t5, img); break;
-    case 4: zfilter_update_kernel<4><<<grid, 256, 0, st>>>(g, C, t5, img); break;
-    case 5: zfilter_update_kernel<5><<<grid, 256, 0, st>>>(g, C, t5, img); break;
-    case 6: zfilter_update_kernel<6><<<grid, 256, 0, st>>>(g, C, t5, img); break;
-    case 7: zfilter_update_kernel<7><<<grid, 256, 0, st>>>(g, C, t5, img); break;
-    case 8: zfilter_update_kernel<8><<<grid, 256, 0, st>>>(g, C, t5, img); break;
+#define GF_ZF(QQ) \
+  case QQ: zfilter_update_kernel<QQ, T><<<grid, 256, 0, st>>>(g, C, t5, img); break;
+    GF_ZF(1) GF_ZF(2) GF_ZF(3) GF_ZF(4) GF_ZF(5) GF_ZF(6) GF_ZF(7) GF_ZF(8)
+#undef GF_ZF
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
+}
+
+cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const Taps5& t5, void* img, cudaStream_t st,
+                                  int img_store) {
+  switch (img_store) {
+    case 0: return zfilter_update_t(g, C, t5, static_cast<float*>(img), st);
+    case 1: return zfilter_update_t(g, C, t5, static_cast<__half*>(img), st);
+    case 2: return zfilter_update_t(g, C, t5, static_cast<__nv_bfloat16*>(img), st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 // The axial filter on its own (voxel 0 keeps the value already in `out`).
@@ -212,22 +237,23 @@ cudaError_t launch_file_to_zfast(const DevGeom& g, const float* in, float* out, 
 
 // z-fast -> file layout; with mask, the output scaling and the radius mask of
 // GFIRST.cu:532-549.
-__global__ void __launch_bounds__(256) zfast_to_file_kernel(const DevGeom g, const float* __restrict__ in,
+template <class T>
+__global__ void __launch_bounds__(256) zfast_to_file_kernel(const DevGeom g, const T* __restrict__ in,
                                                             float scale, int mask, float* __restrict__ out) {
-  __shared__ float T[32][33];
+  __shared__ float Tt[32][33];
   const int x0 = blockIdx.x * 32, y = blockIdx.y, z0 = blockIdx.z * 32;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int RES = g.res;
   for (int i = w; i < 32; i += 8) {
     const int x = x0 + i;
-    T[i][lane] = (x < RES) ? in[((size_t)y * RES + x) * g.nzp + z0 + lane] : 0.f;
+    Tt[i][lane] = (x < RES) ? img_ld(in + ((size_t)y * RES + x) * g.nzp + z0 + lane) : 0.f;
   }
   __syncthreads();
   const int RESM = RES / 2;
   for (int j = w; j < 32; j += 8) {
     const int z = z0 + j, x = x0 + lane;
     if (z >= g.nzs || x >= RES) continue;
-    float v = T[lane][j];
+    float v = Tt[lane][j];
     if (mask) {
       const float dist = (float)((x - RESM) * (x - RESM) + (y - RESM) * (y - RESM) - (RESM - 1) * (RESM - 1));
       v = (dist > 0.f) ? 0.f : __fmul_rn(v, scale);
@@ -236,15 +262,23 @@ __global__ void __launch_bounds__(256) zfast_to_file_kernel(const DevGeom g, con
   }
 }
 
-cudaError_t launch_zfast_to_file(const DevGeom& g, const float* in, float scale, int mask, float* out,
-                                 cudaStream_t st) {
+cudaError_t launch_zfast_to_file(const DevGeom& g, const void* in, float scale, int mask, float* out,
+                                 cudaStream_t st, int in_store) {
   dim3 grid((g.res + 31) / 32, g.res, g.nzp / 32);
-  zfast_to_file_kernel<<<grid, 256, 0, st>>>(g, in, scale, mask, out);
+  switch (in_store) {
+    case 0: zfast_to_file_kernel<<<grid, 256, 0, st>>>(g, static_cast<const float*>(in), scale, mask, out); break;
+    case 1: zfast_to_file_kernel<<<grid, 256, 0, st>>>(g, static_cast<const __half*>(in), scale, mask, out); break;
+    case 2:
+      zfast_to_file_kernel<<<grid, 256, 0, st>>>(g, static_cast<const __nv_bfloat16*>(in), scale, mask, out);
+      break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
 // CreateInitialCylinder, GFIRST_CPU_Kernels.cpp:35-56, z-fast.
-__global__ void cylinder_kernel(const DevGeom g, float val, float* out) {
+template <class T>
+__global__ void cylinder_kernel(const DevGeom g, float val, T* out) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   const size_t n = (size_t)g.res * g.res * g.nzp;
   if (i >= n) return;
@@ -253,12 +287,18 @@ __global__ void cylinder_kernel(const DevGeom g, float val, float* out) {
   const int y = colidx / g.res, x = colidx - y * g.res;
   const int h = g.res / 2;
   const long long r2 = (long long)(x - h) * (x - h) + (long long)(y - h) * (y - h);
-  out[i] = (z < g.nzs && r2 <= (long long)h * h) ? val : 0.f;
+  img_st(out + i, (z < g.nzs && r2 <= (long long)h * h) ? val : 0.f);
 }
 
-cudaError_t launch_cylinder(const DevGeom& g, float val, float* out, cudaStream_t st) {
+cudaError_t launch_cylinder(const DevGeom& g, float val, void* out, cudaStream_t st, int out_store) {
   const size_t n = (size_t)g.res * g.res * g.nzp;
-  cylinder_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, val, out);
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  switch (out_store) {
+    case 0: cylinder_kernel<<<nb, 256, 0, st>>>(g, val, static_cast<float*>(out)); break;
+    case 1: cylinder_kernel<<<nb, 256, 0, st>>>(g, val, static_cast<__half*>(out)); break;
+    case 2: cylinder_kernel<<<nb, 256, 0, st>>>(g, val, static_cast<__nv_bfloat16*>(out)); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

@@ -61,16 +61,18 @@ inline cudaError_t allow_max_smem(K k) {
 
 // ---- image kernels (gf_image.cu) ----
 // out = XY PSF of `in`; with `den` the input is the update ratio in/den.
-cudaError_t launch_conv_xy(const DevGeom& g, const float* in, const float* den, const Taps9& t, float* out,
-                           cudaStream_t st);
+cudaError_t launch_conv_xy(const DevGeom& g, const void* in, const float* den, const Taps9& t, float* out,
+                           cudaStream_t st, int in_store = 0);
 // img *= axial_filter(C), then the edge-slice copy; in place.
-cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const Taps5& t5, float* img, cudaStream_t st);
+// img elements: in_store/img_store/out_store 0 FP32, 1 FP16, 2 BF16 (mode-1 doubles image)
+cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const Taps5& t5, void* img, cudaStream_t st,
+                                  int img_store = 0);
 // Axial filter alone, z-fast in/out (voxel 0 keeps out's value).
 cudaError_t launch_zfilter(const DevGeom& g, const float* C, const Taps5& t5, float* out, cudaStream_t st);
 cudaError_t launch_file_to_zfast(const DevGeom& g, const float* in, float* out, cudaStream_t st);
-cudaError_t launch_zfast_to_file(const DevGeom& g, const float* in, float scale, int mask, float* out,
-                                 cudaStream_t st);
-cudaError_t launch_cylinder(const DevGeom& g, float val, float* out, cudaStream_t st);
+cudaError_t launch_zfast_to_file(const DevGeom& g, const void* in, float scale, int mask, float* out,
+                                 cudaStream_t st, int in_store = 0);
+cudaError_t launch_cylinder(const DevGeom& g, float val, void* out, cudaStream_t st, int out_store = 0);
 cudaError_t launch_max_nonneg(const DevGeom& g, const float* img, float* d_max, cudaStream_t st);
 cudaError_t launch_bilateral(const DevGeom& g, const float* in, const float* ref, const float* d_max_ref,
                              float max_ref, int r, float sigmai, const float* gtab, float* out, cudaStream_t st);

@@ -63,7 +63,7 @@ gf_status gf_recon::project_all(const float* img_zfast, float* proj_full) {
 gf_status gf_recon::init_images() {
   gf_ctx* c = ctx;
   cudaStream_t st = c->stream;
-  GF_LAUNCH(c, launch_cylinder(c->dg, 1.0f, img[0], st));
+  GF_LAUNCH(c, launch_cylinder(c->dg, 1.0f, img[0], st, p.image_storage));
   GF_LAUNCH(c, launch_cylinder(c->dg, p.mode == 1 ? 0.0f : 1.0f, img[1], st));
   if (p.mode == 3) {
     GF_LAUNCH(c, launch_conv_xy(c->dg, img[1], nullptr, g_fw, psf, st));
@@ -83,7 +83,7 @@ gf_status gf_recon::subiteration(int t, int s) {
   const int na = pl.sub_nang[s];
   const int64_t off = pl.sub_off[s];
   stage_begin(GF_STAGE_PSF);
-  GF_LAUNCH(c, launch_conv_xy(c->dg, img[t], nullptr, g_fw, psf, st));
+  GF_LAUNCH(c, launch_conv_xy(c->dg, img[t], nullptr, g_fw, psf, st, t == 0 ? p.image_storage : 0));
   stage_end();
   FpArgs a = c->fp_args(s, psf);
   if (p.mode == 3 && t == 1) {
@@ -112,7 +112,7 @@ gf_status gf_recon::subiteration(int t, int s) {
   stage_end();
   stage_begin(GF_STAGE_UPDATE);
   GF_LAUNCH(c, launch_conv_xy(c->dg, numer, denom, g_bw, ctmp, st));
-  GF_LAUNCH(c, launch_zfilter_update(c->dg, ctmp, g5, img[t], st));
+  GF_LAUNCH(c, launch_zfilter_update(c->dg, ctmp, g5, img[t], st, t == 0 ? p.image_storage : 0));
   stage_end();
   if (t == 1 && s == pl.nsub - 1) {
     // GFIRST.cu:512-524: r=4, sigma3D=0.75, sigmaI=0.025, max_ref over the doubles image
@@ -138,6 +138,7 @@ gf_status gf_recon_defaults(int32_t mode, gf_recon_params* out) {
   out->scale_d = (float)(3.70e-4 * 162.0);
   out->scale_t = (float)(3.70e-4 * 162.0);
   out->storage = GF_STORE_F32;
+  out->image_storage = GF_STORE_F32;
   return GF_OK;
 }
 
@@ -147,6 +148,10 @@ gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out)
   if (prm->mode < 0 || prm->mode > 3) return set_error(GF_ERR_ARG, "mode must be 0..3");
   if (prm->niter < 0) return set_error(GF_ERR_ARG, "niter must be >= 0");
   if (prm->storage < GF_STORE_F32 || prm->storage > GF_STORE_BF16) return set_error(GF_ERR_ARG, "unknown storage");
+  if (prm->image_storage < GF_STORE_F32 || prm->image_storage > GF_STORE_BF16)
+    return set_error(GF_ERR_ARG, "unknown image storage");
+  if (prm->image_storage != GF_STORE_F32 && prm->mode != 1)
+    return set_error(GF_ERR_ARG, "16-bit image storage is for mode 1 only");
   GF_CK(cudaSetDevice(c->device));
   gf_recon* r = new gf_recon();
   r->ctx = c;
@@ -160,7 +165,9 @@ gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out)
   gf_status st;
 #define ALLOC(ptr, n) \
   if ((st = r->alloc_t((size_t)(n), &(ptr))) != GF_OK) return fail(st)
-  ALLOC(r->img[0], pl.nvoxp);
+  // the doubles image: FP32, or 16-bit elements (mode 1, image_storage)
+  if ((st = r->alloc((size_t)pl.nvoxp * (prm->image_storage == GF_STORE_F32 ? 4 : 2), (void**)&r->img[0])) != GF_OK)
+    return fail(st);
   ALLOC(r->proj_ref, pl.ndata);
   if (prm->mode >= 1) {
     ALLOC(r->img[1], pl.nvoxp);
@@ -236,8 +243,9 @@ static gf_status load_impl(gf_recon* r, const float* h_image, const float* h_dsi
   // STEP 1: projection of a unit cylinder -> proj_ref (GFIRST.cu:151-184).  It
   // depends on the geometry alone, so later loads of this reconstruction keep it.
   if (!r->cyl_proj_ready) {
-    if ((s = ck(launch_cylinder(c->dg, 1.0f, r->img[0], st), "cylinder")) != GF_OK) return done(s);
-    if ((s = r->project_all(r->img[0], r->proj_ref)) != GF_OK) return done(s);
+    // the unit cylinder in the FP32 PSF buffer (the doubles image may be 16-bit)
+    if ((s = ck(launch_cylinder(c->dg, 1.0f, r->psf, st), "cylinder")) != GF_OK) return done(s);
+    if ((s = r->project_all(r->psf, r->proj_ref)) != GF_OK) return done(s);
     r->cyl_proj_ready = true;
   }
   // STEP 2: data (GFIRST.cu:207-260)
@@ -365,7 +373,8 @@ gf_status gf_recon_get_image(gf_recon* r, int32_t type, int32_t scaled, float* h
   float* tmp = nullptr;
   GF_CK(cudaMallocAsync(&tmp, pl.nvox * sizeof(float), c->stream));
   const float scale = type == 0 ? r->p.scale_d : r->p.scale_t;
-  cudaError_t e = launch_zfast_to_file(c->dg, r->img[type], scale, scaled ? 1 : 0, tmp, c->stream);
+  cudaError_t e = launch_zfast_to_file(c->dg, r->img[type], scale, scaled ? 1 : 0, tmp, c->stream,
+                                       type == 0 ? r->p.image_storage : 0);
   if (e == cudaSuccess) e = cudaMemcpyAsync(h_out, tmp, pl.nvox * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
   cudaFreeAsync(tmp, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

@@ -222,6 +222,7 @@ gf_status gf_recon_bytes(const gf_geometry* gg, int32_t nsub, const gf_recon_par
   if (!make_plan(geo, nsub, &pl, &err)) return set_error(GF_ERR_GEOMETRY, err);
   const int64_t v = pl.nvoxp * 4, d = pl.ndata * 4, all = pl.all_elems();
   int64_t b = v + d + 64 * 1024;  // image, proj_ref, context tables
+  if (p->image_storage != GF_STORE_F32) b -= pl.nvoxp * 2;  // 16-bit doubles image
   if (p->mode == 0) {
     b += pl.nvox * 4;  // staging
   } else {

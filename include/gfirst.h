@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define GF_ABI_VERSION 1
+#define GF_ABI_VERSION 2
 
 typedef enum gf_status {
   GF_OK = 0,
@@ -186,6 +186,11 @@ typedef struct gf_recon_params {
   int32_t storage; /* per-subset (ratio, mask) sinogram storage: GF_STORE_F32
                       (the reference's precision), GF_STORE_F16 or
                       GF_STORE_BF16; arithmetic stays FP32 */
+  int32_t image_storage; /* storage of the doubles image between
+                            sub-iterations, mode 1 only: GF_STORE_F32 (the
+                            reference), GF_STORE_F16 or GF_STORE_BF16 (every
+                            update rounds the image to 16 bits; arithmetic
+                            stays FP32) */
 } gf_recon_params;
 
 enum { GF_STORE_F32 = 0, GF_STORE_F16 = 1, GF_STORE_BF16 = 2 };

@@ -613,6 +613,32 @@ def test_reduced_precision_ratio_storage(gf, storage, tol):
     assert rel(ref.image(0), exact) < IMG_TOL
 
 
+@pytest.mark.parametrize("storage,tol", [("f16", 1e-3), ("bf16", 1e-2)])
+def test_reduced_precision_image_storage(gf, storage, tol):
+    """The doubles image kept in 16 bits between sub-iterations (mode 1),
+    arithmetic in FP32: every multiplicative update rounds the image, so the
+    error against the FP64 oracle grows with the updates (measured: FP16
+    6.4e-4, BF16 4.9e-3 after 10 sub-iterations)."""
+    geo = case("tinyb")
+    d = parsed("tinyb")
+    exact = gfo.Oracle(geo, "f64").recon(1, nsub=2, niter=5, dsino=d["dsino"], norm=d["norm"])["img_d"]
+    ctx = gf.Context(gf.Geometry(*geo), nsub=2)
+    errs = []
+    for niter in (1, 5):
+        r = gf.Recon(ctx, 1, niter=niter, image_storage=storage)
+        r.load(dsino=d["dsino"], norm=d["norm"])
+        r.iterate(niter)
+        ref = gf.Recon(ctx, 1, niter=niter)
+        ref.load(dsino=d["dsino"], norm=d["norm"])
+        ref.iterate(niter)
+        errs.append(rel(r.image(0), ref.image(0)))
+    err = rel(r.image(0), exact)
+    print(f"image storage {storage}: vs FP32 after 1/5 iterations {errs}, vs FP64 after 5 {err:.3e}")
+    assert err < tol, err
+    with pytest.raises(gf.GfError):
+        gf.Recon(ctx, 2, image_storage=storage)  # 16-bit images are for mode 1 only
+
+
 # ---------------------------------------------------------------- serving
 def _requests(gf):
     reqs = []
