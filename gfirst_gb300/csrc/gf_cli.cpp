@@ -15,6 +15,8 @@
 //                      event (gf_read_vlor_endpoints) instead of int32 bins
 //   --storage f32|f16|bf16   element type of the per-subset ratio sinogram
 //                            (arithmetic stays FP32; default f32)
+//   --image-storage f32|f16|bf16   element type of the doubles image between
+//                                  sub-iterations (mode 1 only; default f32)
 //   --tune             pick the projectors' tile shapes by timing first
 #include <chrono>
 #include <cstdio>
@@ -31,7 +33,7 @@ static int usage() {
   printf("3 Inputs --> Reconstruction Doubles & Triples [Input = Sinog_Doubles + Sinog_Triples + Sinog_Normalization] \n");
   printf("4 Inputs --> VLOR reconstruction [Input = Sinog_Doubles + Sinog_Triples + Sinog_Normalization + Vlor_file] \n");
   printf("options: --geometry res,nzs,nrad,nang,span,nseg,pitch,diam,fov --subsets S --iterations N "
-         "--write-every K --device D --vlor-endpoints --storage f32|f16|bf16 --tune\n");
+         "--write-every K --device D --vlor-endpoints --storage f32|f16|bf16 --image-storage f32|f16|bf16 --tune\n");
   return 0;
 }
 
@@ -45,7 +47,7 @@ int main(int argc, char** argv) {
   gf_geometry_reference(&g);
   int nsub = 1, niter = -1, every = 20, device = 0;
   bool vlor_endpoints = false, tune = false;
-  int storage = GF_STORE_F32;
+  int storage = GF_STORE_F32, image_storage = GF_STORE_F32;
   std::vector<std::string> files;
   for (int i = 1; i < argc; i++) {
     std::string a = argv[i];
@@ -75,13 +77,14 @@ int main(int argc, char** argv) {
       vlor_endpoints = true;
     } else if (a == "--tune") {
       tune = true;
-    } else if (a == "--storage") {
-      const std::string v = val("--storage");
-      if (v == "f32") storage = GF_STORE_F32;
-      else if (v == "f16") storage = GF_STORE_F16;
-      else if (v == "bf16") storage = GF_STORE_BF16;
+    } else if (a == "--storage" || a == "--image-storage") {
+      const std::string v = val(a.c_str());
+      int* dst = a == "--storage" ? &storage : &image_storage;
+      if (v == "f32") *dst = GF_STORE_F32;
+      else if (v == "f16") *dst = GF_STORE_F16;
+      else if (v == "bf16") *dst = GF_STORE_BF16;
       else {
-        fprintf(stderr, "gfirst: --storage wants f32, f16 or bf16\n");
+        fprintf(stderr, "gfirst: %s wants f32, f16 or bf16\n", a.c_str());
         return 2;
       }
     } else if (a == "-h" || a == "--help") {
@@ -101,6 +104,7 @@ int main(int argc, char** argv) {
   gf_recon_defaults(mode, &p);
   if (niter >= 0) p.niter = niter;
   p.storage = storage;
+  p.image_storage = image_storage;
   if (tune) {
     int32_t R, chunk, warps;
     if ((st = gf_tune(ctx, &R, &chunk, &warps)) != GF_OK) return die("gf_tune", st);

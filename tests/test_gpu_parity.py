@@ -360,14 +360,16 @@ def test_cli_end_to_end_matches_reference(gf, tmp_path):
 
 
 def test_cli_storage_and_tune_options(gf, tmp_path):
-    """`--tune` keeps the results; `--storage bf16` stays close to FP32 (mode 1)."""
+    """`--tune` keeps the results; `--storage bf16` and `--image-storage f16`
+    stay close to FP32 (mode 1)."""
     name = "tinyb"
     geo = case(name)
     for k, v in inputs.case_files(name).items():
         (tmp_path / k).write_bytes(v)
     gs = ",".join(str(x) for x in geo)
     imgs = {}
-    for tag, extra in (("plain", []), ("tuned", ["--tune"]), ("bf16", ["--storage", "bf16"])):
+    for tag, extra in (("plain", []), ("tuned", ["--tune"]), ("bf16", ["--storage", "bf16"]),
+                       ("img16", ["--image-storage", "f16"])):
         d = tmp_path / tag
         d.mkdir()
         cmd = [str(gf.CLI_PATH), "--geometry", gs, "--subsets", "3", "--iterations", "20", *extra,
@@ -377,6 +379,7 @@ def test_cli_storage_and_tune_options(gf, tmp_path):
         imgs[tag] = np.fromfile(d / "img_GPU_D_ITER20.raw", np.float32)
     assert rel(imgs["tuned"], imgs["plain"]) < 1e-6
     assert rel(imgs["bf16"], imgs["plain"]) < 1e-2
+    assert rel(imgs["img16"], imgs["plain"]) < 1e-2
 
 
 # ---------------------------------------------------------------- full preclinical size
