@@ -992,7 +992,7 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--cpu-steps", type=int, default=16)
+    ap.add_argument("--cpu-steps", type=int, default=12)
     ap.add_argument("--workload", default="recon", choices=["recon", "frames", "serving", "triples", "small", "cli"])
     ap.add_argument("--events", type=int, default=2_000_000)
     ap.add_argument("--fp32-oracle", type=int, default=1, help="triples: also compare with the FP32 oracle")
