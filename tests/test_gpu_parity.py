@@ -135,6 +135,52 @@ def test_projectors_across_axial_sizes(gf, geo):
     assert rel(proj.download(), o.fp(img, 3, 2)) < FP_TOL
 
 
+def _random_geometries(n, seed=2024):
+    """Small scanner geometries drawn at random (seeded); the ones the plane
+    formula rejects are skipped."""
+    import gfirst_gb300 as gf_
+
+    rs = np.random.RandomState(seed)
+    out = []
+    while len(out) < n:
+        res = int(rs.choice([8, 12, 16, 20, 24, 32]))
+        nzs = int(rs.randint(3, 70))
+        nrad = int(rs.randint(5, 40))
+        nang = int(rs.randint(4, 40))
+        span = int(rs.choice([1, 3, 5, 7]))
+        nseg = int(rs.choice([1, 3, 5, 7, 9]))
+        pitch = float(rs.uniform(1.2, 2.2))
+        fov = res * float(rs.uniform(0.6, 1.0))
+        diam = fov * 1.657758
+        nsub = int(rs.choice([1, 2, 3, 4]))
+        if nsub > nang:
+            continue
+        geo = (res, nzs, nrad, nang, span, nseg, pitch, diam, fov)
+        try:
+            gf_.sizes(gf_.Geometry(*geo))
+        except gf_.GfError:
+            continue
+        out.append((geo, nsub))
+    return out
+
+
+@pytest.mark.parametrize("k", range(16))
+def test_projectors_on_random_geometries(gf, k):
+    geo, nsub = _random_geometries(16)[k]
+    o = gfo.Oracle(geo)
+    ctx = gf.Context(gf.Geometry(*geo), nsub=nsub)
+    sub = k % nsub
+    img = image(o, 300 + k)
+    proj = ctx.array(o.ndata).zero()
+    ctx.forward_project(ctx.put(img), sub, proj)
+    assert rel(proj.download(), o.fp(img, nsub, sub)) < FP_TOL, geo
+    corr, calib = corr_calib(o, 400 + k)
+    numer, denom = ctx.array(o.nvox), ctx.array(o.nvox)
+    ctx.back_project(ctx.put(corr), ctx.put(calib), sub, numer, denom)
+    wn, wd = o.bp(corr, calib, nsub, sub)
+    assert np.array_equal(numer.download(), wn) and np.array_equal(denom.download(), wd), geo
+
+
 # ---------------------------------------------------------------- update chain
 @pytest.mark.parametrize("name", ["tiny", "small"])
 def test_psf_and_update_bit_exact(gf, name):
