@@ -181,6 +181,26 @@ def test_projectors_on_random_geometries(gf, k):
     assert np.array_equal(numer.download(), wn) and np.array_equal(denom.download(), wd), geo
 
 
+@pytest.mark.parametrize("k,mode", [(0, 1), (1, 3), (4, 2), (8, 3), (11, 1), (14, 3)])
+def test_recon_on_random_geometries(gf, k, mode):
+    geo, nsub = _random_geometries(16)[k]
+    o = gfo.Oracle(geo)
+    rs = np.random.RandomState(500 + k)
+    nd = o.ndata
+    dsino = np.concatenate([rs.poisson(3.0, nd), rs.uniform(0, 0.2, nd)]).astype(np.float32)
+    tsino = np.concatenate([rs.poisson(0.5, nd), np.zeros(nd)]).astype(np.float32)
+    norm = rs.uniform(0.8, 1.2, nd).astype(np.float32)
+    ev = rs.randint(1, nd + 1, size=(max(nd // 4, 8), 2)).astype(np.int32)
+    want = o.recon(mode, nsub=nsub, niter=2, dsino=dsino, tsino=tsino, norm=norm, ev=ev)
+    ctx = gf.Context(gf.Geometry(*geo), nsub=nsub)
+    r = gf.Recon(ctx, mode, niter=2)
+    r.load(dsino=dsino, tsino=tsino if mode >= 2 else None, norm=norm, events=ev if mode == 3 else None)
+    r.iterate(2)
+    assert rel(r.image(0), want["img_d"]) < IMG_TOL, geo
+    if mode >= 2:
+        assert rel(r.image(1), want["img_t"]) < IMG_TOL, geo
+
+
 # ---------------------------------------------------------------- update chain
 @pytest.mark.parametrize("name", ["tiny", "small"])
 def test_psf_and_update_bit_exact(gf, name):
