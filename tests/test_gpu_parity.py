@@ -754,6 +754,31 @@ def test_server_results_same_alone_and_in_mix(gf):
     assert 0 < st["p50_ms"] <= st["p99_ms"]
 
 
+def test_server_isolates_a_failing_request(gf):
+    """A request that passes admission but cannot be set up on the device
+    (300 image planes, above the supported 256) fails alone; the requests
+    queued around it complete with their usual results.  (A subset count
+    above the angle count is refused already at submission.)"""
+    d = parsed("tinyb")
+    g = gf.Geometry(*case("tinyb"))
+    bad = gf.Geometry(*((g.res, 300) + g.tuple()[2:]))
+    alone = _alone(gf, ("recon", g, d["dsino"], d["norm"], 2, 2))
+    srv = gf.Server(1 << 30, max_active=2)
+    with pytest.raises(gf.GfError):
+        srv.submit_recon(g, d["dsino"], d["norm"], g.nang + 1, 2)
+    ids = [srv.submit_recon(g, d["dsino"], d["norm"], 2, 2),
+           srv.submit_recon(bad, d["dsino"], d["norm"], 2, 2),
+           srv.submit_recon(g, d["dsino"], d["norm"], 2, 2)]
+    out0, _ = srv.wait(ids[0])
+    with pytest.raises(gf.GfError):
+        srv.wait(ids[1])
+    out2, _ = srv.wait(ids[2])
+    st = srv.stats()
+    srv.close()
+    assert np.array_equal(out0, alone) and np.array_equal(out2, alone)
+    assert st["completed"] == 2 and st["failed"] == 1
+
+
 def test_server_rejects_request_beyond_its_budget(gf):
     d = parsed("small")
     srv = gf.Server(1 << 20, max_active=2)
