@@ -27,7 +27,9 @@
 // coordinate is taken with a round-down add of 1.5*2^23 instead of the
 // conversion pipe.  The views of a segment run with the segment's row chunk
 // count fixed at compile time (one switch per segment), so staging issues no
-// instructions for chunks beyond the segment's rows.
+// instructions for chunks beyond the segment's rows; for a segment narrower
+// than the column, a view's voxel work issues only the lane chunks that can
+// hold its in-range voxels (voxel_window).
 #include "gf_kernels.h"
 
 namespace gf {
@@ -47,11 +49,11 @@ __device__ __forceinline__ float2 lerp2(float2 a, float2 b, float2 w) { return _
 
 // The voxels of one view: each lane's voxels interpolate between two staged
 // rows along z and add to their (NUMER, DENOM) sums.
-template <int Q>
+template <int Q, int LO, int HI>
 __device__ __forceinline__ void voxel_views(float2 (&acc)[Q], const float (&fiz)[Q], const float2* rows, float t,
                                             float zlo, float zhi, int zm1, int nzs, int lane) {
 #pragma unroll
-  for (int q = 0; q < Q; q++) {
+  for (int q = LO; q <= HI; q++) {
     // z = float(iz) + yrot*fz + 0.5f, GFIRST_GPU_Kernels.cu:148
     const float z = __fadd_rn(__fadd_rn(fiz[q], t), 0.5f);
     // every lane of chunks 0..Q-2 holds a voxel (NZP = NZS rounded up to 32)
@@ -68,6 +70,33 @@ __device__ __forceinline__ void voxel_views(float2 (&acc)[Q], const float (&fiz)
       const float2 v = lerp2(rows[j], rows[j + 1], make_float2(be, be));
       // GFIRST_GPU_Kernels.cu:157: a negative interpolated value (a gap) zeroes both
       if (!(v.y < 0.f || v.x < 0.f)) acc[q] = __fadd2_rn(acc[q], v);
+    }
+  }
+}
+
+// The voxels of one view for a segment whose rows fill NCH lane chunks.  Its
+// in-range voxels (z = iz + t + 0.5 rounded, in [zlo, zhi), nzs - 2*zmin =
+// nrow - 2 <= 32*NCH - 2 of them at most, consecutive in iz since the rounded
+// z is monotone) lie in the NCH + 1 chunks from the chunk of
+// izlo = floor(zlo - t - 1): izlo is at most two below the first in-range
+// voxel, so the last one is at most 32*(izlo/32) + 31 + 2 + 32*NCH - 2.  When
+// that window is narrower than the column, only its chunks issue (one
+// compile-time instance per window start); the per-voxel range test stays.
+template <int Q, int NCH>
+__device__ __forceinline__ void voxel_window(float2 (&acc)[Q], const float (&fiz)[Q], const float2* rows, float t,
+                                             float zlo, float zhi, int zm1, int nzs, int lane) {
+  constexpr int W = NCH + 1;
+  if constexpr (W >= Q) {
+    voxel_views<Q, 0, Q - 1>(acc, fiz, rows, t, zlo, zhi, zm1, nzs, lane);
+  } else {
+    const int izlo = max(__float2int_rd(__fsub_rn(__fsub_rn(zlo, t), 1.0f)), 0);
+    switch (min(izlo >> 5, Q - W)) {
+#define GF_VW(L) \
+  case L:        \
+    if constexpr (L <= Q - W) voxel_views<Q, L, L + W - 1>(acc, fiz, rows, t, zlo, zhi, zm1, nzs, lane); \
+    break;
+      GF_VW(0) GF_VW(1) GF_VW(2) GF_VW(3) GF_VW(4) GF_VW(5) GF_VW(6)
+#undef GF_VW
     }
   }
 }
@@ -116,7 +145,7 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
         e = my[tl + 1];
         load(e);
       }
-      voxel_views<Q>(acc, fiz, rows, t, zlo, zhi, zm1, nzs, lane);
+      voxel_window<Q, NCH>(acc, fiz, rows, t, zlo, zhi, zm1, nzs, lane);
     }
   }
 }
