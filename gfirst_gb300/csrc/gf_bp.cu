@@ -112,9 +112,9 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
   const int nrow = sg.nplanes + 2;
   // The rows of view tl + 1 are loaded into the registers that view tl's rows
   // have just left, before view tl's voxels, so their latency overlaps that
-  // work.  FP32 pairs need the larger register budget of bp_kernel's launch
-  // bounds for it (1.39 ms at 80 registers vs 1.79 ms squeezed into 64; 1.44
-  // ms without prefetch); 16-bit pairs fit in 64 (1.35 ms).
+  // work.  FP32 pairs need a larger register budget than 64 for it (1.39 ms
+  // at 80 registers vs 1.79 ms squeezed into 64; 1.44 ms without prefetch);
+  // 16-bit pairs fit in 64 (1.35 ms).
   {
     Pair c0[NCH], c1[NCH];
     auto load = [&](const int4& e) {
@@ -151,7 +151,7 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
 }
 
 template <int Q, int STORE>
-__global__ void __launch_bounds__(256, STORE == 0 ? 3 : 4) bp_kernel(const BpArgs a, int rmax) {
+__device__ __forceinline__ void bp_column(const BpArgs& a, int rmax) {
   using Pair = typename PairT<STORE>::type;
   const Pair* cc = static_cast<const Pair*>(a.corrcal);
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -207,6 +207,28 @@ __global__ void __launch_bounds__(256, STORE == 0 ? 3 : 4) bp_kernel(const BpArg
   }
 }
 
+// Register budgets.  The kernel hides its latencies with resident warps: up
+// to 160 slices FP32 pairs are capped at 72 registers (seven 4-warp blocks
+// per SM; a few bytes spill) and 16-bit pairs at 64 (eight blocks) -- 1.3355
+// vs 1.3430 ms and 1.2420 vs 1.2637 ms under the launch bounds below.
+// Deeper columns keep those launch bounds (80 and 64 registers), which
+// spill less there.
+template <int Q, int STORE>
+__global__ void __launch_bounds__(256) __maxnreg__(STORE == 0 ? 72 : 64) bp_kernel(const BpArgs a, int rmax) {
+  bp_column<Q, STORE>(a, rmax);
+}
+
+template <int Q, int STORE>
+__global__ void __launch_bounds__(256, STORE == 0 ? 3 : 4) bp_kernel_deep(const BpArgs a, int rmax) {
+  bp_column<Q, STORE>(a, rmax);
+}
+
+template <int Q, int STORE>
+static void (*bp_entry())(BpArgs, int) {
+  if constexpr (Q <= 5) return bp_kernel<Q, STORE>;
+  else return bp_kernel_deep<Q, STORE>;
+}
+
 cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st) {
   if (warps < 1 || warps > 8) return cudaErrorInvalidValue;
   const int Q = a.g.nzp / 32;
@@ -216,7 +238,7 @@ cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st) {
   void (*k)(BpArgs, int) = nullptr;
   switch (a.storage * 16 + Q) {
 #define GF_BP_CASE(S, QQ) \
-  case S * 16 + QQ: k = bp_kernel<QQ, S>; break;
+  case S * 16 + QQ: k = bp_entry<QQ, S>(); break;
     GF_BP_CASE(0, 1) GF_BP_CASE(0, 2) GF_BP_CASE(0, 3) GF_BP_CASE(0, 4)
     GF_BP_CASE(0, 5) GF_BP_CASE(0, 6) GF_BP_CASE(0, 7) GF_BP_CASE(0, 8)
     GF_BP_CASE(1, 1) GF_BP_CASE(1, 2) GF_BP_CASE(1, 3) GF_BP_CASE(1, 4)
