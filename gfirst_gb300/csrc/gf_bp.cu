@@ -112,16 +112,19 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
   const int nrow = sg.nplanes + 2;
   // The rows of view tl + 1 are loaded into the registers that view tl's rows
   // have just left, before view tl's voxels, so their latency overlaps that
-  // work.  FP32 pairs need a larger register budget than 64 for it (1.39 ms
-  // at 80 registers vs 1.79 ms squeezed into 64; 1.44 ms without prefetch);
-  // 16-bit pairs fit in 64 (1.35 ms).
+  // work.  16-bit pairs prefetch every chunk within 64 registers.  FP32 pairs
+  // prefetch their first three chunks and load the others while staging: that
+  // fits 64 registers too, and the eighth resident block per SM hides more
+  // than the exposed loads cost (1.294 ms; all chunks prefetched at 72
+  // registers, seven blocks: 1.336 ms; at 80 registers, six blocks: 1.343 ms).
   {
-    Pair c0[NCH], c1[NCH];
+    constexpr int PF = (sizeof(Pair) == 8 && NCH > 3) ? 3 : NCH;
+    Pair c0[PF], c1[PF];
     auto load = [&](const int4& e) {
       const Pair* p0 = cc + e.x + sg.blk;
       const Pair* p1 = cc + e.y + sg.blk;
 #pragma unroll
-      for (int k = 0; k < NCH; k++) {
+      for (int k = 0; k < PF; k++) {
         const int r = lane + 32 * k;
         if (k < NCH - 1 || r < nrow) {
           c0[k] = __ldg(p0 + r);
@@ -135,10 +138,15 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
       const float2 al2 = make_float2(__int_as_float(e.z), __int_as_float(e.z));
       const float t = __fmul_rn(__int_as_float(e.w), sg.fz);  // yrot*fz
       __syncwarp();  // every lane is done reading the previous view's rows
+      const Pair* q0 = cc + e.x + sg.blk;
+      const Pair* q1 = cc + e.y + sg.blk;
 #pragma unroll
       for (int k = 0; k < NCH; k++) {
         const int r = lane + 32 * k;
-        if (k < NCH - 1 || r < nrow) rows[r] = lerp2(pair_f(c0[k]), pair_f(c1[k]), al2);
+        if (k < NCH - 1 || r < nrow) {
+          if (k < PF) rows[r] = lerp2(pair_f(c0[k < PF ? k : 0]), pair_f(c1[k < PF ? k : 0]), al2);
+          else rows[r] = lerp2(pair_f(__ldg(q0 + r)), pair_f(__ldg(q1 + r)), al2);
+        }
       }
       __syncwarp();
       if (tl + 1 < na) {
@@ -208,13 +216,19 @@ __device__ __forceinline__ void bp_column(const BpArgs& a, int rmax) {
 }
 
 // Register budgets.  The kernel hides its latencies with resident warps: up
-// to 160 slices FP32 pairs are capped at 72 registers (seven 4-warp blocks
-// per SM; a few bytes spill) and 16-bit pairs at 64 (eight blocks) -- 1.3355
-// vs 1.3430 ms and 1.2420 vs 1.2637 ms under the launch bounds below.
-// Deeper columns keep those launch bounds (80 and 64 registers), which
-// spill less there.
+// to 160 slices both pair types are capped at 64 registers (eight 4-warp
+// blocks per SM, no spill; FP32 with the shallower prefetch above) -- 1.296
+// and 1.245 ms against 1.343 and 1.264 ms under the launch bounds of
+// bp_kernel_deep (six and eight blocks).  The cap is a constant that depends
+// on the template argument, so it stands beside the 256-thread bound (both
+// reach the compiled kernel); the cap alone, or a (128, 8) launch bound,
+// schedules worse: 1.340 and 1.266 ms.  Deeper columns keep the launch
+// bounds below, which spill less there.
+template <int STORE>
+constexpr int bp_reg_cap = 64;
+
 template <int Q, int STORE>
-__global__ void __launch_bounds__(256) __maxnreg__(STORE == 0 ? 72 : 64) bp_kernel(const BpArgs a, int rmax) {
+__global__ void __launch_bounds__(256) __maxnreg__(bp_reg_cap<STORE>) bp_kernel(const BpArgs a, int rmax) {
   bp_column<Q, STORE>(a, rmax);
 }
 

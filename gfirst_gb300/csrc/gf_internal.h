@@ -63,7 +63,7 @@ struct gf_ctx {
   float gtab_sigma = -1.f;
   // scratch of the operator entry points, allocated on first use
   int64_t launches = 0;  // kernels launched by this context
-  int bp_warps = 4;      // back-projector warps (columns) per block (seven blocks per SM fit the FP32 register cap)
+  int bp_warps = 4;      // back-projector warps (columns) per block (eight blocks per SM fit the register cap)
   float* s_img = nullptr;
   float* s_img2 = nullptr;
   float* s_numer = nullptr;
