@@ -29,7 +29,6 @@ __global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const T* 
                                                       const float* __restrict__ den, const Taps9 G,
                                                       float* __restrict__ out) {
   __shared__ float S[16][16][32];
-  __shared__ float Y[8][16][32];
   const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int x0 = blockIdx.x * 8, y0 = blockIdx.y * 8, z = blockIdx.z * 32 + lane;
   const int RES = g.res, NZP = g.nzp;
@@ -68,14 +67,16 @@ __global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const T* 
     }
   }
   __syncthreads();
-#pragma unroll 4
+  // the y pass of row ty over the 16 halo columns stays in this thread's
+  // registers: the x pass below reads only its own row and slice
+  float yv[16];
+#pragma unroll
   for (int xx = 0; xx < 16; xx++) {
     float acc = __fmul_rn(S[ty][xx][lane], G.c[0]);
 #pragma unroll
     for (int k = 1; k < 9; k++) acc = __fadd_rn(acc, __fmul_rn(S[ty + k][xx][lane], G.c[k]));
-    Y[ty][xx][lane] = acc;
+    yv[xx] = acc;
   }
-  __syncthreads();
   const int y = y0 + ty;
   if (y >= RES) return;
 #pragma unroll
@@ -84,9 +85,9 @@ __global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const T* 
     if (x >= RES) break;
     float v;
     if (x > 3 && x < RES - 4) {
-      v = __fmul_rn(Y[ty][xo][lane], G.c[0]);
+      v = __fmul_rn(yv[xo], G.c[0]);
 #pragma unroll
-      for (int k = 1; k < 9; k++) v = __fadd_rn(v, __fmul_rn(Y[ty][xo + k][lane], G.c[k]));
+      for (int k = 1; k < 9; k++) v = __fadd_rn(v, __fmul_rn(yv[xo + k], G.c[k]));
     } else {
       v = S[ty + 4][xo + 4][lane];
     }
