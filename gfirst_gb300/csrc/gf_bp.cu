@@ -29,7 +29,11 @@
 // count fixed at compile time (one switch per segment), so staging issues no
 // instructions for chunks beyond the segment's rows; for a segment narrower
 // than the column, a view's voxel work issues only the lane chunks that can
-// hold its in-range voxels (voxel_window).
+// hold its in-range voxels (voxel_window).  What keeps issue below peak is
+// dependency latency, which resident warps hide, so up to 160 slices the
+// kernel is held to 64 registers (eight 4-warp blocks per SM): the next view's
+// rows are prefetched into registers during the current view's voxels, all
+// of them for 16-bit pairs and the first three row chunks for FP32 pairs.
 #include "gf_kernels.h"
 
 namespace gf {
