@@ -45,6 +45,7 @@ struct Job {
   bool in_flight = false;
   int iters = 0;
   int state = 0;  // 0 queued, 1 active, 2 done
+  bool claimed = false;  // a gf_server_wait is waiting for it
   gf_status status = GF_OK;
   std::string err;
 };
@@ -86,10 +87,12 @@ static void release(Job* j) {
 }
 
 void gf_server::finish(Job* j, gf_status st) {
+  // the failing call's message, before the clean-up calls below run
+  const std::string err = st != GF_OK ? std::string(gf_last_error()) : std::string();
   release(j);
   std::lock_guard<std::mutex> lk(mu);
   j->status = st;
-  if (st != GF_OK) j->err = gf_last_error();
+  if (st != GF_OK) j->err = err;
   j->t_done = now_ms();
   j->state = 2;
   bytes_in_use -= j->bytes;
@@ -309,6 +312,9 @@ gf_status gf_server_wait(gf_server* s, int64_t id, double* latency_ms) {
   auto it = s->jobs.find(id);
   if (it == s->jobs.end()) return set_error(GF_ERR_ARG, "unknown request id");
   Job* j = it->second;
+  // one waiter per request: the waiter that returns deletes it
+  if (j->claimed) return set_error(GF_ERR_ARG, "request is already being waited for");
+  j->claimed = true;
   s->cv_done.wait(lk, [&] { return j->state == 2; });
   // the request is finished and nothing else refers to it: forget it here, so
   // a long-running server holds only requests that are queued, running or

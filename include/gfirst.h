@@ -290,7 +290,8 @@ gf_status gf_server_create(int32_t device, int64_t budget_bytes, int32_t max_act
 void gf_server_destroy(gf_server* s);
 gf_status gf_server_submit(gf_server* s, const gf_request* req, int64_t* id);
 /* Blocks until request id completes; its status (GF_OK or the failure).  The
- * server then forgets the request: each id is waited for once. */
+ * server then forgets the request: each id is waited for once, by one thread
+ * (a second concurrent wait for the same id returns GF_ERR_ARG). */
 gf_status gf_server_wait(gf_server* s, int64_t id, double* latency_ms);
 gf_status gf_server_get_stats(gf_server* s, gf_server_stats* out);
 
