@@ -139,15 +139,17 @@ def committed_traffic() -> dict:
 
 
 # ----------------------------------------------------------------- CPU (oracle)
-def cpu_subiterations(nsteps: int, warmup: int, dsino=None, norm=None) -> dict:
+def cpu_subiterations(nsteps: int, warmup: int, dsino=None, norm=None, tag: str = "f32", snapshots=()) -> dict:
     """Times sub-iterations of the CPU oracle (FP32 restatement of the reference
     path, OpenMP over all host cores): psf, projection of one subset, ratio, back
-    projection, update.  Test infrastructure, used only as the baseline."""
+    projection, update.  Test infrastructure, used only as the baseline and as
+    the checker: the returned "images" hold the oracle's image after each
+    sub-iteration count listed in `snapshots` (tag "f64": the FP64 oracle)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import gfo
 
     gfo.build()
-    o = gfo.Oracle(GEOM)
+    o = gfo.Oracle(GEOM, tag)
     if dsino is None:
         proj = np.zeros(o.ndata, np.float32)
         img = phantom()
@@ -174,15 +176,19 @@ def cpu_subiterations(nsteps: int, warmup: int, dsino=None, norm=None) -> dict:
         numer, denom = o.bp(corr, calib, NSUB, s)
         img = o.update(img, numer, denom, 1.5)
 
+    images = {}
     for k in range(warmup):
         step(k)
     t0 = time.perf_counter()
     for k in range(nsteps):
         step(warmup + k)
+        if warmup + k + 1 in snapshots:
+            images[warmup + k + 1] = np.array(img, copy=True)
     dt = time.perf_counter() - t0
     return {"value": nsteps / dt, "unit": UNIT, "cores": gfo.cores(), "kind": "port", "seconds": dt,
             "sample": f"{nsteps} sub-iteration(s) of the preclinical workload (one subset each: psf, projection, "
-                      f"ratio, back projection, update), CPU FP32 oracle, OpenMP"}
+                      f"ratio, back projection, update), CPU {tag.upper()} oracle, OpenMP",
+            "images": images}
 
 
 def run_reference(args) -> int:
@@ -190,6 +196,7 @@ def run_reference(args) -> int:
     if rank != 0:
         return 0
     cpu = cpu_subiterations(args.steps, args.warmup)
+    cpu.pop("images", None)
     line = {"metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * cpu["seconds"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA, "impl": "reference",
@@ -389,14 +396,41 @@ def run_gpu(args) -> int:
                               "ms_per_step": 1000.0 * dt_seq / args.e2e_steps,
                               "path": "gf_recon_load + gf_recon_iterate(2) + gf_recon_get_image, one "
                                       "reconstruction, each step after the previous one"}}
-        for r in recs:
-            r.close()
+        for rr in recs:
+            rr.close()
         ctx_b.close()
         gf.lib().gf_host_free(hp)
 
-    cpu = None
+    cpu, accuracy = None, None
     if rank == 0 and world == 1 and args.cpu_steps > 0:
-        cpu = cpu_subiterations(args.cpu_steps, 0, dsino, norm)
+        # The CPU oracle's sub-iterations are the baseline and the checker: the
+        # GPU image after the same sub-iterations from the same start is
+        # compared with the FP32 oracle's, and, on a shorter sample, with the
+        # FP64 oracle's (the accuracy bound is stated against FP64).
+        n64 = min(args.fp64_steps, args.cpu_steps)
+        cpu = cpu_subiterations(args.cpu_steps, 0, dsino, norm, snapshots={args.cpu_steps, n64})
+        img32 = cpu.pop("images")
+
+        def gpu_image_after(n):
+            gf._ck(gf.lib().gf_recon_restart(r.h))
+            for _ in range(n):
+                r.subiteration()
+            return r.image(0)
+
+        def rel(a, b):
+            return float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b.astype(np.float64)))
+
+        accuracy = {"subiterations": args.cpu_steps,
+                    "rel_l2_vs_fp32_oracle": rel(gpu_image_after(args.cpu_steps), img32[args.cpu_steps]),
+                    "tolerance": 1e-3,
+                    "sample": f"doubles image after the first {args.cpu_steps} sub-iterations of the headline "
+                              f"reconstruction (same inputs, same start); FP64 oracle on the first {n64}"}
+        if n64 > 0:
+            img64 = cpu_subiterations(n64, 0, dsino, norm, tag="f64", snapshots={n64})["images"][n64]
+            g64 = gpu_image_after(n64)
+            accuracy["fp64_subiterations"] = n64
+            accuracy["rel_l2_vs_fp64_oracle"] = rel(g64, img64)
+            accuracy["fp32_oracle_vs_fp64_oracle"] = rel(img32[n64], img64)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -411,7 +445,7 @@ def run_gpu(args) -> int:
                            "tile_shapes": tuned},
                 "rays_per_s": value * ndata / NSUB, "ray_samples_per_s": value * ndata / NSUB * (g.res + 1),
                 "voxel_views_per_s": value * nvox * (g.nang // NSUB) * g.nseg,
-                "stages": stage, "roofline": roofline,
+                "stages": stage, "roofline": roofline, "accuracy": accuracy,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
         print(json.dumps(line))
     r.close()
@@ -993,6 +1027,8 @@ def main() -> int:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=12)
+    ap.add_argument("--fp64-steps", type=int, default=4, help="sub-iterations of the FP64 oracle for the "
+                    "headline's accuracy field (0: FP32 oracle only)")
     ap.add_argument("--workload", default="recon", choices=["recon", "frames", "serving", "triples", "small", "cli"])
     ap.add_argument("--events", type=int, default=2_000_000)
     ap.add_argument("--fp32-oracle", type=int, default=1, help="triples: also compare with the FP32 oracle")

@@ -127,6 +127,13 @@ def segment_table(g: Geometry):
     return idz, zmin, acc
 
 
+def bp_staged_rows(g: Geometry) -> dict:
+    """The per-view back projector's staged-row buffer (gf_bp_staged_rows)."""
+    lo, hi, rb = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    _ck(lib().gf_bp_staged_rows(ctypes.byref(g.c()), ctypes.byref(lo), ctypes.byref(hi), ctypes.byref(rb)))
+    return {"pad_lo": lo.value, "pad_hi": hi.value, "rbuf": rb.value}
+
+
 def lor_index(g: Geometry, seg: int, iz0: int, theta: int, ird: int) -> int:
     out = ctypes.c_int64()
     _ck(lib().gf_lor_index(ctypes.byref(g.c()), seg, iz0, theta, ird, ctypes.byref(out)))
@@ -218,6 +225,10 @@ class Context:
         n = ctypes.c_int64()
         _ck(lib().gf_kernel_launches(self.h, ctypes.byref(n)))
         return n.value
+
+    def set_bp_form(self, form: str) -> None:
+        """Back projector's axial interpolation: "voxel" (GF_BP_PER_VOXEL) or "view" (GF_BP_PER_VIEW)."""
+        _ck(lib().gf_set_bp_form(self.h, {"voxel": 0, "view": 1}[form]))
 
     def tune(self) -> dict:
         r, lc, w = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()

@@ -7,7 +7,12 @@
 // a join event per frame back to the origin.  The graph is then launched once
 // per iteration.  Replay is exact because a sub-iteration's launches depend
 // only on the frame's (type, subset) cursor, which returns to the start
-// after a full iteration, and every buffer is updated in place.
+// after a full iteration, and every buffer is updated in place.  The graph
+// holds each frame's launch parameters as captured (tile shapes, the mode-3
+// event count and buffers); a frame whose context was retuned or whose load
+// changed them since (gf_ctx::gen, gf_recon::gen) makes the next iterate
+// capture the graph again.
+#include <utility>
 #include <vector>
 
 #include "gf_internal.h"
@@ -22,7 +27,23 @@ struct gf_batch {
   std::vector<cudaEvent_t> joins;
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
+  std::vector<std::pair<int64_t, int64_t>> cap_gen;  // (context, reconstruction) generations at capture
 };
+
+static bool stale(const gf_batch* b) {
+  for (size_t i = 0; i < b->frames.size(); i++) {
+    const gf_recon* r = b->frames[i];
+    if (b->cap_gen[i] != std::make_pair(r->ctx->gen, r->gen)) return true;
+  }
+  return false;
+}
+
+static void drop_graph(gf_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
 
 extern "C" {
 
@@ -55,8 +76,7 @@ void gf_batch_destroy(gf_batch* b) {
   if (!b) return;
   cudaSetDevice(b->device);
   if (b->origin) cudaStreamSynchronize(b->origin);
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  if (b->graph) cudaGraphDestroy(b->graph);
+  drop_graph(b);
   for (auto ev : b->joins)
     if (ev) cudaEventDestroy(ev);
   if (b->fork) cudaEventDestroy(b->fork);
@@ -103,6 +123,8 @@ static gf_status capture(gf_batch* b) {
   if (e2 != cudaSuccess) return cuda_error(e2, "cudaStreamEndCapture");
   b->graph = g;
   GF_CK(cudaGraphInstantiate(&b->exec, g, 0));
+  b->cap_gen.clear();
+  for (gf_recon* r : b->frames) b->cap_gen.emplace_back(r->ctx->gen, r->gen);
   // capturing advanced every frame's host cursor by one iteration, but the
   // captured work has not run: the first replay below is that iteration
   for (gf_recon* r : b->frames) {
@@ -119,6 +141,11 @@ gf_status gf_batch_iterate(gf_batch* b, int32_t n, int32_t use_graph) {
     for (int it = 0; it < n; it++)
       for (gf_recon* r : b->frames) GF_TRY(gf_recon_iterate(r, 1));
     return GF_OK;
+  }
+  if (b->exec && stale(b)) {
+    // a replay still queued on the origin stream may use the old graph
+    GF_CK(cudaStreamSynchronize(b->origin));
+    drop_graph(b);
   }
   if (!b->exec) GF_TRY(capture(b));
   // the frames' own streams may hold work queued outside the graph

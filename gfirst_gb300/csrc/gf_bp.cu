@@ -105,9 +105,46 @@ __device__ __forceinline__ void voxel_window(float2 (&acc)[Q], const float (&fiz
   }
 }
 
+// The voxels of one view, per-view form: the axial fraction and the row
+// offset of the view are shared by every voxel of the column (z = iz + t +
+// 0.5 is taken without the per-voxel rounding, which moves a weight by at
+// most one unit in the last place of iz + t), so lane chunk q reads staged
+// rows rv[32q] and rv[32q + 1] at fixed offsets from one per-view pointer.
+// Voxels outside the segment's plane range read sentinel rows (or a
+// sentinel pad row with weight >= 1/2): their interpolated mask is negative
+// and the gap rule skips them, as the reference's range test does.
+template <int Q, int LO, int HI>
+__device__ __forceinline__ void voxel_views_fast(float2 (&acc)[Q], const float2* rv, float2 be2) {
+#pragma unroll
+  for (int q = LO; q <= HI; q++) {
+    const float2 v = lerp2(rv[32 * q], rv[32 * q + 1], be2);
+    if (!(v.y < 0.f || v.x < 0.f)) acc[q] = __fadd2_rn(acc[q], v);
+  }
+}
+
+// voxel_window for the per-view form (same lane-chunk window).
+template <int Q, int NCH>
+__device__ __forceinline__ void voxel_window_fast(float2 (&acc)[Q], const float2* rv, float2 be2, float t,
+                                                  float zlo) {
+  constexpr int W = NCH + 1;
+  if constexpr (W >= Q) {
+    voxel_views_fast<Q, 0, Q - 1>(acc, rv, be2);
+  } else {
+    const int izlo = max(__float2int_rd(__fsub_rn(__fsub_rn(zlo, t), 1.0f)), 0);
+    switch (min(izlo >> 5, Q - W)) {
+#define GF_VWF(L) \
+  case L:         \
+    if constexpr (L <= Q - W) voxel_views_fast<Q, L, L + W - 1>(acc, rv, be2); \
+    break;
+      GF_VWF(0) GF_VWF(1) GF_VWF(2) GF_VWF(3) GF_VWF(4) GF_VWF(5) GF_VWF(6)
+#undef GF_VWF
+    }
+  }
+}
+
 // One segment's views with its row chunk count NCH fixed at compile time, so
 // the staging issues exactly the chunks the segment's rows occupy.
-template <int Q, int NCH, class Pair>
+template <int Q, int NCH, bool FAST, class Pair>
 __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fiz)[Q], const Pair* cc,
                                               const int4* my, float2* rows, const DevSeg& sg, int na, int nzs,
                                               int lane) {
@@ -157,12 +194,20 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
         e = my[tl + 1];
         load(e);
       }
-      voxel_window<Q, NCH>(acc, fiz, rows, t, zlo, zhi, zm1, nzs, lane);
+      if constexpr (FAST) {
+        // z = iz + t + 0.5 lies between rows floor(t) + iz - zm1 and the next
+        const float ft = floorf(t);
+        const float be = __fsub_rn(t, ft);
+        const float2* rv = rows + ((int)ft - zm1) + lane;
+        voxel_window_fast<Q, NCH>(acc, rv, make_float2(be, be), t, zlo);
+      } else {
+        voxel_window<Q, NCH>(acc, fiz, rows, t, zlo, zhi, zm1, nzs, lane);
+      }
     }
   }
 }
 
-template <int Q, int STORE>
+template <int Q, int STORE, bool FAST>
 __device__ __forceinline__ void bp_column(const BpArgs& a, int rmax) {
   using Pair = typename PairT<STORE>::type;
   const Pair* cc = static_cast<const Pair*>(a.corrcal);
@@ -175,6 +220,13 @@ __device__ __forceinline__ void bp_column(const BpArgs& a, int rmax) {
   const int iy = colidx / g.res, ix = colidx - iy * g.res;
   int4* my = reinterpret_cast<int4*>(smraw) + wib * a.na;
   float2* rows = reinterpret_cast<float2*>(reinterpret_cast<int4*>(smraw) + nwarps * a.na) + wib * rmax;
+  const float2 sentinel = make_float2(-1000.f, -1000.f);
+  if constexpr (FAST) {
+    // rmax = rbuf here: every row starts at the gap sentinel; views stage
+    // theirs from offset pad_lo
+    for (int r = lane; r < rmax; r += 32) rows[r] = sentinel;
+    rows += a.pad_lo;
+  }
   // per angle: radial texels, weight and yrot (GFIRST_GPU_Kernels.cu:136-147)
   const float xv = __fsub_rn((float)ix, g.resm), yv = __fsub_rn((float)iy, g.resm);
   for (int tl = lane; tl < a.na; tl += 32) {
@@ -200,10 +252,17 @@ __device__ __forceinline__ void bp_column(const BpArgs& a, int rmax) {
   }
   for (int s = 0; s < g.nseg; s++) {
     const DevSeg sg = g.seg[s];
+    if constexpr (FAST) {
+      // rows past this segment's back to the sentinel (a wider segment left
+      // its rows there); the first view's warp barrier orders these stores
+      __syncwarp();
+      const int nrow = sg.nplanes + 2;
+      for (int r = nrow + lane; r < rmax - a.pad_lo; r += 32) rows[r] = sentinel;
+    }
     switch ((sg.nplanes + 2 + 31) >> 5) {
 #define GF_SEG(N) \
   case N:         \
-    if constexpr (N <= Q + 1) segment_views<Q, N>(acc, fiz, cc, my, rows, sg, a.na, g.nzs, lane); \
+    if constexpr (N <= Q + 1) segment_views<Q, N, FAST>(acc, fiz, cc, my, rows, sg, a.na, g.nzs, lane); \
     break;
       GF_SEG(1) GF_SEG(2) GF_SEG(3) GF_SEG(4) GF_SEG(5) GF_SEG(6) GF_SEG(7) GF_SEG(8) GF_SEG(9)
 #undef GF_SEG
@@ -233,30 +292,42 @@ constexpr int bp_reg_cap = 64;
 
 template <int Q, int STORE>
 __global__ void __launch_bounds__(256) __maxnreg__(bp_reg_cap<STORE>) bp_kernel(const BpArgs a, int rmax) {
-  bp_column<Q, STORE>(a, rmax);
+  bp_column<Q, STORE, false>(a, rmax);
 }
 
 template <int Q, int STORE>
 __global__ void __launch_bounds__(256, STORE == 0 ? 3 : 4) bp_kernel_deep(const BpArgs a, int rmax) {
-  bp_column<Q, STORE>(a, rmax);
+  bp_column<Q, STORE, false>(a, rmax);
+}
+
+// The per-view form needs no per-voxel z registers; the same caps apply.
+template <int Q, int STORE>
+__global__ void __launch_bounds__(256) __maxnreg__(bp_reg_cap<STORE>) bp_fast_kernel(const BpArgs a, int rmax) {
+  bp_column<Q, STORE, true>(a, rmax);
 }
 
 template <int Q, int STORE>
-static void (*bp_entry())(BpArgs, int) {
-  if constexpr (Q <= 5) return bp_kernel<Q, STORE>;
-  else return bp_kernel_deep<Q, STORE>;
+__global__ void __launch_bounds__(256, STORE == 0 ? 3 : 4) bp_fast_kernel_deep(const BpArgs a, int rmax) {
+  bp_column<Q, STORE, true>(a, rmax);
+}
+
+template <int Q, int STORE>
+static void (*bp_entry(bool fast))(BpArgs, int) {
+  if constexpr (Q <= 5) return fast ? bp_fast_kernel<Q, STORE> : bp_kernel<Q, STORE>;
+  else return fast ? bp_fast_kernel_deep<Q, STORE> : bp_kernel_deep<Q, STORE>;
 }
 
 cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st) {
   if (warps < 1 || warps > 8) return cudaErrorInvalidValue;
   const int Q = a.g.nzp / 32;
-  const int rmax = a.g.nzs + 2;
+  if (a.fast && (a.pad_lo < 0 || a.rbuf < a.pad_lo + a.g.nzs + 2)) return cudaErrorInvalidValue;
+  const int rmax = a.fast ? a.rbuf : a.g.nzs + 2;
   dim3 grid((a.g.res * a.g.res + warps - 1) / warps);
   size_t smem = (size_t)warps * (a.na * sizeof(int4) + rmax * sizeof(float2));
   void (*k)(BpArgs, int) = nullptr;
   switch (a.storage * 16 + Q) {
 #define GF_BP_CASE(S, QQ) \
-  case S * 16 + QQ: k = bp_entry<QQ, S>(); break;
+  case S * 16 + QQ: k = bp_entry<QQ, S>(a.fast != 0); break;
     GF_BP_CASE(0, 1) GF_BP_CASE(0, 2) GF_BP_CASE(0, 3) GF_BP_CASE(0, 4)
     GF_BP_CASE(0, 5) GF_BP_CASE(0, 6) GF_BP_CASE(0, 7) GF_BP_CASE(0, 8)
     GF_BP_CASE(1, 1) GF_BP_CASE(1, 2) GF_BP_CASE(1, 3) GF_BP_CASE(1, 4)

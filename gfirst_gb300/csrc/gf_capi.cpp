@@ -117,7 +117,43 @@ FpArgs gf_ctx::fp_args(int subset, const float* img_zfast) const {
   return a;
 }
 
+BpArgs gf_ctx::bp_args(int subset, const void* cc, float* numer, float* denom, int storage) const {
+  BpArgs b{};
+  b.g = dg;
+  b.subset = subset;
+  b.na = plan.sub_nang[subset];
+  b.corrcal = cc;
+  b.numer = numer;
+  b.denom = denom;
+  b.storage = storage;
+  b.fast = bp_form == GF_BP_PER_VIEW ? 1 : 0;
+  b.pad_lo = bpp.pad_lo;
+  b.rbuf = bpp.rbuf;
+  return b;
+}
+
 extern "C" {
+
+gf_status gf_set_bp_form(gf_ctx* c, int32_t form) {
+  if (!c) return set_error(GF_ERR_ARG, "null context");
+  if (form != GF_BP_PER_VOXEL && form != GF_BP_PER_VIEW) return set_error(GF_ERR_ARG, "unknown back-projector form");
+  if (form != c->bp_form) c->gen++;  // captured graphs hold the form
+  c->bp_form = form;
+  return GF_OK;
+}
+
+gf_status gf_bp_staged_rows(const gf_geometry* g, int32_t* pad_lo, int32_t* pad_hi, int32_t* rbuf) {
+  Geom geo;
+  if (!to_geom(g, &geo)) return set_error(GF_ERR_ARG, "null geometry");
+  Plan p;
+  std::string err;
+  if (!make_plan(geo, 1, &p, &err)) return set_error(GF_ERR_GEOMETRY, err);
+  const BpPads b = bp_fast_pads(p);
+  if (pad_lo) *pad_lo = b.pad_lo;
+  if (pad_hi) *pad_hi = b.pad_hi;
+  if (rbuf) *rbuf = b.rbuf;
+  return GF_OK;
+}
 
 gf_status gf_kernel_launches(const gf_ctx* c, int64_t* n) {
   if (!c || !n) return set_error(GF_ERR_ARG, "null argument");
@@ -218,6 +254,7 @@ gf_status gf_create(const gf_geometry* g, int32_t nsubsets, int32_t device, gf_c
     cudaGetLastError();
   }
   gf_ctx* c = new gf_ctx();
+  c->bpp = bp_fast_pads(plan);
   c->plan = std::move(plan);
   c->fps = std::move(fps);
   c->device = device;
@@ -440,7 +477,7 @@ gf_status gf_back_project(gf_ctx* c, const float* d_corr, const float* d_calib, 
   GF_TRY(c->ensure_scratch());
   const int na = c->plan.sub_nang[subset];
   GF_LAUNCH(c, launch_corrcal_from_file(c->dg, c->d_rowmap, subset, na, d_corr, d_calib, c->s_cc, c->stream));
-  BpArgs b{c->dg, subset, na, c->s_cc, c->s_numer, c->s_denom, 0};
+  BpArgs b = c->bp_args(subset, c->s_cc, c->s_numer, c->s_denom, 0);
   GF_LAUNCH(c, launch_bp(b, c->bp_warps, c->stream));
   GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_numer, 1.f, 0, d_numer, c->stream));
   GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_denom, 1.f, 0, d_denom, c->stream));

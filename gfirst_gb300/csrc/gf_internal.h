@@ -63,7 +63,12 @@ struct gf_ctx {
   float gtab_sigma = -1.f;
   // scratch of the operator entry points, allocated on first use
   int64_t launches = 0;  // kernels launched by this context
+  // Bumped whenever a launch parameter that a captured graph holds changes
+  // (the projectors' tile shapes, gf_tune); gf_batch recaptures on a change.
+  int64_t gen = 0;
   int bp_warps = 4;      // back-projector warps (columns) per block (eight blocks per SM fit the register cap)
+  int bp_form = GF_BP_PER_VOXEL;  // back projector's axial interpolation (gf_set_bp_form)
+  gf::BpPads bpp;        // staged-row buffer of the per-view form
   float* s_img = nullptr;
   float* s_img2 = nullptr;
   float* s_numer = nullptr;
@@ -77,6 +82,7 @@ struct gf_ctx {
   gf_status ensure_scratch();
   gf_status ensure_gtab(float sigma3d);
   gf::FpArgs fp_args(int subset, const float* img_zfast) const;
+  gf::BpArgs bp_args(int subset, const void* corrcal, float* numer, float* denom, int storage) const;
 };
 
 struct gf_recon {
@@ -111,6 +117,9 @@ struct gf_recon {
   int64_t subs_done = 0;
   int cur_type = 0, cur_sub = 0;
   int64_t launches_per_iteration = 0;  // kernels in one captured iteration
+  // Bumped when a load changes what an iteration's launches capture (the
+  // mode-3 event count or event buffers); gf_batch recaptures on a change.
+  int64_t gen = 0;
 
   // stage profiling
   struct StageEv {
@@ -124,6 +133,8 @@ struct gf_recon {
   void stage_end();
 
   gf_status alloc(size_t bytes, void** p);
+  // Returns an owned buffer to the device pool (stream-ordered) and forgets it.
+  void release(void* p);
   template <class T> gf_status alloc_t(size_t n, T** q) {
     return alloc(n * sizeof(T), reinterpret_cast<void**>(q));
   }

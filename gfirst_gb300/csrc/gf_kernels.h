@@ -41,6 +41,10 @@ struct BpArgs {
   float* numer;            // z-fast
   float* denom;            // z-fast
   int storage;             // corrcal pair type, as FpArgs::storage
+  // Axial interpolation: 0 per voxel with the reference's rounding (the
+  // oracle's sums bit for bit), 1 per view (BpPads; within 1e-5 of it).
+  int fast;
+  int pad_lo, rbuf;        // fast form: staged-row buffer per warp (BpPads)
 };
 cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st);
 // Lets kernel k use up to the device's opt-in shared memory per block.  Every

@@ -116,6 +116,41 @@ bool make_fp_schedule(const Plan& p, int R, int lc, FpSchedule* out) {
   return true;
 }
 
+BpPads bp_fast_pads(const Plan& p) {
+  // Mirrors the kernel's choice of lane chunks (all Q of them, or the NCH + 1
+  // from the chunk of floor(zmin - t - 1)) and its row index j = iz +
+  // floor(t) - (zmin - 1), and takes the extremes of j and j + 1 over every
+  // piece of t: the functions change only where t or zmin - t crosses an
+  // integer, so each integer is sampled on both sides (a float evaluation in
+  // the kernel can fall only into an adjacent piece) and at its midpoint.
+  const int Q = p.NZP / 32;
+  const double ymax = std::sqrt(2.0) * (double)p.resm + 1.0;
+  int lo = 0, hi = 0;
+  for (const Seg& sg : p.seg) {
+    const int nrow = sg.nplanes + 2;
+    const int W = (nrow + 31) / 32 + 1;
+    const double tmax = ymax * std::fabs((double)sg.fz) + 1.0;
+    for (int m = (int)std::floor(-tmax) - 1; m <= (int)std::ceil(tmax) + 1; m++) {
+      for (double t : {m - 1e-3, (double)m, m + 1e-3, m + 0.5}) {
+        const int k = (int)std::floor(t) - (sg.zmin - 1);
+        int c0 = 0, c1 = Q - 1;
+        if (W < Q) {
+          const int izlo = std::max((int)std::floor((double)sg.zmin - t - 1.0), 0);
+          c0 = std::min(izlo >> 5, Q - W);
+          c1 = c0 + W - 1;
+        }
+        lo = std::max(lo, -(32 * c0 + k));
+        hi = std::max(hi, (32 * c1 + 31 + k + 1) - (nrow - 1));
+      }
+    }
+  }
+  BpPads b;
+  b.pad_lo = lo + 2;
+  b.pad_hi = hi + 2;
+  b.rbuf = b.pad_lo + (p.g.nzs + 2) + b.pad_hi;
+  return b;
+}
+
 int fp_default_R(const Plan& p) {
   for (int R : {9, 17, 25, 33}) {
     FpSchedule f;

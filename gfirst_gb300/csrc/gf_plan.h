@@ -66,6 +66,19 @@ struct FpSchedule {
 bool make_fp_schedule(const Plan& p, int R, int lc, FpSchedule* out);
 int fp_default_R(const Plan& p);
 
+// Staged-row buffer of the back projector's per-view form: each warp stages a
+// view's rows at offset pad_lo of a buffer of rbuf (corr, calib) pairs, the
+// rest held at the -1000 gap sentinel.  A lane chunk reads its two rows at
+// an offset fixed per view, so voxels outside the segment's plane range read
+// sentinels there (or the segment's own sentinel pad rows with weight >=
+// 1/2), which the gap rule skips as the range test would.  pad_lo and the
+// rows past the widest segment cover every row any issued lane chunk reads,
+// for every axial shift |t| <= |yrot| * |fz| the geometry allows.
+struct BpPads {
+  int pad_lo = 0, pad_hi = 0, rbuf = 0;
+};
+BpPads bp_fast_pads(const Plan& p);
+
 // Sinogram bin of (segment, plane, angle, radial), GFIRST.cu:175-176.
 inline int64_t lor_index(const Plan& p, int s, int iz0, int t, int r) {
   return ((int64_t)(iz0 - p.seg[s].zmin) + p.seg[s].acc) * ((int64_t)p.g.nrad * p.g.nang) + (int64_t)t * p.g.nrad + r;

@@ -31,6 +31,17 @@ gf_status gf_recon::alloc(size_t bytes, void** q) {
   return GF_OK;
 }
 
+void gf_recon::release(void* q) {
+  if (!q) return;
+  for (size_t i = 0; i < owned.size(); i++) {
+    if (owned[i].p == q) {
+      cudaFreeAsync(q, ctx->stream);
+      owned.erase(owned.begin() + (long)i);
+      return;
+    }
+  }
+}
+
 void gf_recon::stage_begin(int stage) {
   if (!prof) return;
   if (ev_used == evs.size()) {
@@ -106,7 +117,7 @@ gf_status gf_recon::subiteration(int t, int s) {
     GF_LAUNCH(c, launch_fp(a, c->fps, st));
     stage_end();
   }
-  BpArgs b{c->dg, s, na, corrcal, numer, denom, p.storage};
+  BpArgs b = c->bp_args(s, corrcal, numer, denom, p.storage);
   stage_begin(GF_STAGE_BP);
   GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
   stage_end();
@@ -260,9 +271,19 @@ static gf_status load_impl(gf_recon* r, const float* h_image, const float* h_dsi
     if ((s = ck(launch_build_dbg(c->dg, c->d_rowmap, s2, r->dbg[1], st), "build triples")) != GF_OK) return done(s);
   }
   if (mode == 3) {
+    if (nevents != r->nev) r->gen++;  // the split's launch holds the count
     r->nev = nevents;
     if (nevents > 0) {
       if (nevents > r->ev_cap) {
+        // the smaller buffers go back to the pool before the larger ones are taken
+        r->release(r->events);
+        r->release(r->vlor_keys);
+        r->release(r->vlor_share);
+        r->events = nullptr;
+        r->vlor_keys = nullptr;
+        r->vlor_share = nullptr;
+        r->ev_cap = 0;
+        r->gen++;
         if ((s = r->alloc_t((size_t)nevents * 2, &r->events)) != GF_OK) return done(s);
         if ((s = r->alloc_t((size_t)nevents * 2, &r->vlor_keys)) != GF_OK) return done(s);
         if ((s = r->alloc_t((size_t)nevents * 2, &r->vlor_share)) != GF_OK) return done(s);

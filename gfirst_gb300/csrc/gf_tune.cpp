@@ -106,7 +106,7 @@ extern "C" gf_status gf_tune(gf_ctx* c, int32_t* fp_run, int32_t* fp_chunk, int3
   int best_w = c->bp_warps;
   float best_bp = 3.0e38f;
   for (int w : {4, 8}) {
-    BpArgs b{c->dg, 0, p.sub_nang[0], c->s_cc, c->s_numer, c->s_denom, 0};
+    BpArgs b = c->bp_args(0, c->s_cc, c->s_numer, c->s_denom, 0);
     float ms = 0.f;
     s = time_it([&] { return launch_bp(b, w, st); }, &ms);
     if (s != GF_OK) return done(s);
@@ -117,6 +117,7 @@ extern "C" gf_status gf_tune(gf_ctx* c, int32_t* fp_run, int32_t* fp_chunk, int3
     }
   }
   c->bp_warps = best_w;
+  c->gen++;  // graphs captured with the old shapes are stale
   if (fp_run) *fp_run = c->fps.R;
   if (fp_chunk) *fp_chunk = c->fps.lc;
   if (bp_warps) *bp_warps = c->bp_warps;

@@ -80,6 +80,25 @@ void gf_destroy(gf_ctx* ctx);
 gf_status gf_set_stream(gf_ctx* ctx, void* cuda_stream);
 gf_status gf_synchronize(gf_ctx* ctx);
 
+/* Axial interpolation of the back projector (BACKWPROJ_K,
+ * GFIRST_GPU_Kernels.cu:148-152: z = float(iz) + yrot*fz + 0.5f per voxel).
+ * GF_BP_PER_VOXEL takes z with that rounding for every voxel, so NUMER and
+ * DENOM are the FP32 oracle's sums bit for bit.  GF_BP_PER_VIEW takes the
+ * axial fraction of yrot*fz once per (column, view) for all voxels of the
+ * column -- an interpolation weight moves by at most one unit in the last
+ * place of iz + yrot*fz (about 1e-5 relative in the sums) -- and lets voxels
+ * outside the segment's planes fall to the gap rule through sentinel rows
+ * instead of a range test.  The reference's own hardware interpolation
+ * quantises these weights to 1/256. */
+enum { GF_BP_PER_VOXEL = 0, GF_BP_PER_VIEW = 1 };
+gf_status gf_set_bp_form(gf_ctx* ctx, int32_t form);
+/* The per-view form's staged-row buffer for a geometry (no device work): a
+ * view's rows sit at offset pad_lo of rbuf (corr, calib) pairs per warp, the
+ * rest hold the gap sentinel; pad_hi rows past a segment's last row are
+ * read.  Shared memory per 4-warp block: 4 * (16 * angles per subset + 8 *
+ * rbuf) bytes. */
+gf_status gf_bp_staged_rows(const gf_geometry* g, int32_t* pad_lo, int32_t* pad_hi, int32_t* rbuf);
+
 /* Device memory helpers for callers without a CUDA runtime of their own. */
 gf_status gf_device_alloc(gf_ctx* ctx, size_t bytes, void** d_ptr);
 gf_status gf_device_free(gf_ctx* ctx, void* d_ptr);
@@ -148,8 +167,9 @@ gf_status gf_vlor_split(gf_ctx* ctx, const int32_t* d_events, int64_t nevents, c
  * voxels) are rejected with GF_ERR_ARG.  Runs on the current device and on
  * `cuda_stream` (NULL: the legacy default stream).  The first call on a
  * device looks up the array's device address; make that call before any
- * stream capture.  All calls share the array: calls whose work overlaps on
- * the GPU race. */
+ * stream capture.  The address is kept for the life of the process, so a
+ * cudaDeviceReset of that device ends this entry point's use there.  All
+ * calls share the array: calls whose work overlaps on the GPU race. */
 gf_status gf_forward_project_noalloc(const gf_geometry* g, int32_t nsubsets, int32_t subset, const float* d_image,
                                      float* d_proj, void* cuda_stream);
 
@@ -271,7 +291,9 @@ typedef struct gf_request {
 } gf_request;
 typedef struct gf_server_stats {
   int64_t submitted, completed, failed, queued, active;
-  double p50_ms, p99_ms, mean_ms, max_ms;  /* submit-to-result latency of completed requests */
+  double p50_ms, p99_ms, mean_ms, max_ms;  /* submit-to-result latency of completed requests;
+                                              p50/p99 from 1 %-wide log bins (within 0.5 %),
+                                              mean and max exact */
   double throughput_per_s;                 /* completed requests / seconds since the first submit */
   int64_t bytes_in_use, peak_bytes, budget_bytes;
   int32_t peak_active;

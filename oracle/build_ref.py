@@ -1,7 +1,8 @@
 """Build the host-emulated reference program into oracle/_ref/.
 
 TEST INFRASTRUCTURE ONLY.  This recipe reads the GFIRST sources where they
-lie (default /root/reference, or $GFIRST_REFERENCE), copies the definitions
+lie ($GFIRST_REFERENCE, else a tree named `reference` beside the repository
+checkout), copies the definitions
 of the functions listed below verbatim into oracle/_ref/*.inc (git-ignored,
 never committed), and compiles them with oracle/ref_shim.h + ref_main.cpp
 into one executable per geometry:
@@ -24,7 +25,15 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REF = Path(os.environ.get("GFIRST_REFERENCE", "/root/reference"))
+
+
+def reference_dir() -> Path:
+    """The GFIRST source tree: $GFIRST_REFERENCE, else `reference` beside the checkout."""
+    env = os.environ.get("GFIRST_REFERENCE")
+    return Path(env) if env else HERE.parent.parent / "reference"
+
+
+REF = reference_dir()
 
 KERNEL_FUNCS = [
     "FORWPROJ_K", "BACKWPROJ_K", "divVxVGPU", "CleanMemoryK", "chequearError",

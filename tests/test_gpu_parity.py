@@ -517,6 +517,93 @@ def test_preclinical_properties(gf, c2):
     assert np.array_equal(n, d) and n.max() > 0  # identical channels give identical sums
 
 
+def _preclinical_data(gf, ctx, seed=1002):
+    """The preclinical configuration's inputs: the seeded mouse-like phantom
+    forward-projected by the library (parity-tested above), normalization gains
+    U(0.85, 1.15), Poisson prompts scaled to 5e7 counts, background 0."""
+    import bench
+
+    P, ndata, nvox = gf.sizes(ctx.g)
+    dimg = ctx.put(bench.phantom(seed))
+    proj = ctx.array(ndata).zero()
+    for s in range(ctx.nsub):
+        ctx.forward_project(dimg, s, proj)
+    return bench.sinogram_from_projection(proj.download(), seed + 1)
+
+
+def test_preclinical_full_iteration_mode1_matches_oracle(gf, c2):
+    """One full iteration (all 16 sub-iterations) of the preclinical
+    configuration -- 128x128x159 image, 4319 planes x 160 angles x 128 bins,
+    Poisson data at 5e7 counts -- against the FP32 oracle on the same inputs
+    (the image bound of 1e-3)."""
+    g, ctx = c2
+    dsino, norm = _preclinical_data(gf, ctx)
+    r = gf.Recon(ctx, 1, niter=1)
+    r.load(dsino=dsino, norm=norm)
+    r.iterate(1)
+    got = r.image(0)
+    want = gfo.Oracle(g.tuple()).recon(1, nsub=16, niter=1, dsino=dsino, norm=norm)
+    assert rel(r.proj_ref(), want["proj_ref"]) < FP_TOL
+    err = rel(got, want["img_d"])
+    print(f"preclinical mode 1, 16 sub-iterations: rel L2 vs FP32 oracle {err:.3e}")
+    assert err < IMG_TOL
+    r.close()
+
+
+def test_preclinical_mode3_reduced_events_matches_oracle(gf):
+    """Mode 3 (doubles sinogram + triples VLOR list) at the preclinical
+    geometry, 8 subsets x 1 iteration (16 sub-iterations and one joint
+    bilateral filter), 200000 VLOR events: both images against the FP32
+    oracle (1e-3)."""
+    g = gf.Geometry.preclinical()
+    ctx = gf.Context(g, nsub=8)
+    dsino, norm = _preclinical_data(gf, ctx, 1102)
+    P, ndata, nvox = gf.sizes(g)
+    rs = np.random.RandomState(1104)
+    prompts = dsino[:ndata]
+    lam_t = 0.04 * prompts + 0.01
+    tsino = np.concatenate([rs.poisson(lam_t), np.zeros(ndata)]).astype(np.float32)
+    w = np.cumsum(prompts.astype(np.float64) + 1e-3)
+    nev = 200000
+    a = np.searchsorted(w, rs.uniform(0, w[-1], nev), side="right")
+    b = rs.randint(0, ndata, nev)
+    ev = (np.stack([a, b], axis=1) + 1).astype(np.int32)
+    ev[::1000, 1] = 0  # rejected by the reference's range test
+    r = gf.Recon(ctx, 3, niter=1)
+    r.load(dsino=dsino, tsino=tsino, norm=norm, events=ev)
+    r.iterate(1)
+    got_d, got_t = r.image(0), r.image(1)
+    want = gfo.Oracle(g.tuple()).recon(3, nsub=8, niter=1, dsino=dsino, tsino=tsino, norm=norm, ev=ev)
+    ed, et = rel(got_d, want["img_d"]), rel(got_t, want["img_t"])
+    print(f"preclinical mode 3: rel L2 vs FP32 oracle doubles {ed:.3e}, triples {et:.3e}")
+    assert ed < IMG_TOL and et < IMG_TOL
+    r.close()
+    ctx.close()
+
+
+def test_bilateral_on_preclinical_phantom_matches_oracle(gf):
+    """The joint bilateral filter on a realistic image: the preclinical
+    phantom as the guide (max_ref from it, as GFIRST.cu:512-524 takes it) and
+    a noisy copy as the input.  The kernel's intensity weight is FP32 __expf
+    where the reference evaluates exp in double; the difference stays far
+    inside the 1e-5 bound."""
+    import bench
+
+    g = gf.Geometry.preclinical()
+    o = gfo.Oracle(g.tuple())
+    ctx = gf.Context(g)
+    ref = bench.phantom(1002)
+    inp = (ref * np.random.RandomState(3).uniform(0.7, 1.3, ref.size)).astype(np.float32)
+    mx = float(ref.max())
+    out = ctx.array(o.nvox)
+    ctx.bilateral(ctx.put(inp), ctx.put(ref), mx, out)
+    got, want = out.download(), o.bilateral(inp, ref, mx)
+    err = rel(got, want)
+    print(f"bilateral, preclinical phantom: rel L2 {err:.3e}, max abs {np.abs(got - want).max():.3e}")
+    assert np.array_equal(got == 0, want == 0)
+    assert err < 1e-5
+
+
 # ---------------------------------------------------------------- VLOR as LOR endpoints
 def endpoint_events(gf, g, pairs):
     return np.stack([np.concatenate([gf.bin_endpoints(g, int(a)), gf.bin_endpoints(g, int(b))]) for a, b in pairs])
@@ -638,6 +725,42 @@ def test_batch_matches_frames_run_alone(gf, graph):
             assert rel(g0, a0) < 1e-6 and rel(g1, a1) < 1e-5
         else:
             assert np.array_equal(g0, a0) and np.array_equal(g1, a1)
+    b.close()
+
+
+def test_batch_recaptures_after_retune_and_reload(gf):
+    """A batch's graph holds each frame's launch parameters as captured.
+    Retuning a frame's context, or reloading a mode-3 frame with fewer and
+    then more VLOR events (a new count, then new buffers), makes the next
+    iterate capture again: the frames still give the images of the same
+    frames run alone."""
+    d = parsed("tinyb")
+    g = gf.Geometry(*case("tinyb"))
+    ev = d["events"]
+    frames = _frames(gf, [(1, 2), (3, 2)])
+    b = gf.Batch([r for _, r in frames])
+    b.iterate(1, graph=True)
+    b.sync()
+    for step, events in ((0, ev[: len(ev) // 2]), (1, np.concatenate([ev, ev[::-1]]))):
+        frames[0][0].tune()
+        frames[1][1].load(dsino=d["dsino"], tsino=d["tsino"], norm=d["norm"], events=events)
+        for _, r in frames:
+            r.restart()
+        b.iterate(2, graph=True)
+        b.sync()
+        c0 = gf.Context(g, nsub=2)
+        c0.tune()
+        a0 = gf.Recon(c0, 1, niter=2)
+        a0.load(dsino=d["dsino"], norm=d["norm"])
+        a0.iterate(2)
+        c1 = gf.Context(g, nsub=2)
+        a1 = gf.Recon(c1, 3, niter=2)
+        a1.load(dsino=d["dsino"], tsino=d["tsino"], norm=d["norm"], events=events)
+        a1.iterate(2)
+        assert np.array_equal(frames[0][1].image(0), a0.image(0)), step
+        assert rel(frames[1][1].image(0), a1.image(0)) < 1e-6, step
+        assert rel(frames[1][1].image(1), a1.image(1)) < 1e-5, step
+        assert np.array_equal(frames[1][1].sinog_vlor(), a1.sinog_vlor()), step
     b.close()
 
 

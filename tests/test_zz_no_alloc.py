@@ -2,7 +2,8 @@
 allocate device memory (a host that owns the whole device memory map, an
 embedding framework with its own pool, code where an allocation would stall
 or be refused).  Its scratch is a fixed file-scope device array instead of
-context buffers; its output must equal gf_forward_project's, call after call.
+context buffers; its output must equal gf_forward_project's, call after call,
+and sit within the projection tolerance of the CPU oracle.
 
 This file is collected last on purpose, so a run that stops at the first
 failure has run every other test before it.
@@ -69,6 +70,8 @@ def test_noalloc_matches_forward_project_twice(gf, name):
         assert st == 0, gf.lib().gf_last_error().decode()
         device_sync()
         got = out.download()
+        oracle = gfo.Oracle(geo).fp(img, nsub, subset)  # bins of other subsets stay 0 in both
+        assert rel(got, oracle) < FP_TOL, f"call {call}: against the CPU oracle"
         assert rel(got, want) < FP_TOL, f"call {call}"
         assert np.array_equal(got, want), f"call {call}: same kernels, same inputs"
 
