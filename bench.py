@@ -151,21 +151,21 @@ def cpu_subiterations(nsteps: int, warmup: int, dsino=None, norm=None, tag: str 
     gfo.build()
     o = gfo.Oracle(GEOM, tag)
     if dsino is None:
-        proj = np.zeros(o.ndata, np.float32)
+        proj = np.zeros(o.ndata, o.dt)
         img = phantom()
         for s in range(NSUB):
             o.fp(img, NSUB, s, out=proj)
         dsino, norm = sinogram_from_projection(proj)
     res = np.float32(GEOM[0])
     data, bg = dsino[: o.ndata] * res, dsino[o.ndata:] * res
-    proj_blank = np.zeros(o.ndata, np.float32)
+    proj_blank = np.zeros(o.ndata, o.dt)
     cyl = o.cylinder(1.0)
     for s in range(NSUB):
         o.fp(cyl, NSUB, s, out=proj_blank)
     calib = o.calib(proj_blank, norm)
     img = o.cylinder(1.0)
-    proj = np.zeros(o.ndata, np.float32)
-    corr = np.zeros(o.ndata, np.float32)
+    proj = np.zeros(o.ndata, o.dt)
+    corr = np.zeros(o.ndata, o.dt)
 
     def step(k: int) -> None:
         nonlocal img
@@ -923,7 +923,12 @@ def run_serving(args) -> int:
     pool of 6 pre-generated noisy sinograms per size).  HBM budget 150 GB.
     Plain: FP32, one request at a time.  Batched: FP16 storage of the ratio
     sinogram, up to 8 requests in flight (continuous batching).  Latency runs
-    from submission to the result in host memory."""
+    from submission to the result in host memory.  With --serve-closed C the
+    same request mix runs as a closed loop instead (--serve-requests of them,
+    C in flight at all times), which measures each arm's capacity rather than
+    the offered rate.  Accuracy: sampled reconstructions of the batched arm
+    against the same requests in the plain arm, and one 64^3 request of each
+    arm against the FP64 oracle (test infrastructure, used as the checker)."""
     import threading
 
     import torch
@@ -960,39 +965,70 @@ def run_serving(args) -> int:
         else:
             reqs.append(("recon", nm, rs.randint(6), 2 + rs.randint(2)))
     budget = 150 * 10**9
+    closed = args.serve_closed > 0
+    if closed:  # a fixed list of requests, kept args.serve_closed in flight: the arms' capacity
+        n = args.serve_requests
+        reqs = reqs[:n] if len(reqs) >= n else (reqs * (n // max(len(reqs), 1) + 1))[:n]
+    # outputs kept for the accuracy comparison: every 8th reconstruction request
+    sample = [i for i, q in enumerate(reqs) if q[0] == "recon"][::8][:24]
+    kept = {}
     out = {}
     for arm, storage, max_active in (("plain", "f32", 1), ("batched", "f16", 8)):
         srv = gf.Server(budget, max_active=max_active)
-        ids = [None] * n
-        ready = threading.Event()
-        t_start = [0.0]
+        lat = {"project": [], "recon": []}
+        lock = threading.Lock()
 
-        def submitter():
-            t0 = time.perf_counter()
-            t_start[0] = t0
-            ready.set()
-            for i, (kind, nm, k, it) in enumerate(reqs):
-                d = arrivals[i] - (time.perf_counter() - t0)
-                if d > 0:
-                    time.sleep(d)
-                g, nsub, sinos, imgs, _ = pool[nm]
-                if kind == "project":
-                    ids[i] = srv.submit_project(g, imgs[k], nsub)
-                else:
-                    ids[i] = srv.submit_recon(g, sinos[k][0], sinos[k][1], nsub, it, storage)
+        def submit(i):
+            kind, nm, k, it = reqs[i]
+            g, nsub, sinos, imgs, _ = pool[nm]
+            if kind == "project":
+                return srv.submit_project(g, imgs[k], nsub)
+            return srv.submit_recon(g, sinos[k][0], sinos[k][1], nsub, it, storage)
+
+        def finish(i, rid):
+            res, ms = srv.wait(rid)
+            with lock:
+                lat[reqs[i][0]].append(ms)
+                if i in sample:
+                    kept[(arm, i)] = np.array(res, copy=True)
 
         clk = clocks_start(0)
-        th = threading.Thread(target=submitter)
-        th.start()
-        ready.wait()
-        lat = {"project": [], "recon": []}
-        for i in range(n):
-            while ids[i] is None:
-                time.sleep(0.0005)
-            _, ms = srv.wait(ids[i])
-            lat[reqs[i][0]].append(ms)
+        t0 = time.perf_counter()
+        if closed:
+            nxt = [0]
+
+            def worker():
+                while True:
+                    with lock:
+                        i = nxt[0]
+                        nxt[0] += 1
+                    if i >= n:
+                        return
+                    finish(i, submit(i))
+
+            ths = [threading.Thread(target=worker) for _ in range(args.serve_closed)]
+            for th in ths:
+                th.start()
+            for th in ths:
+                th.join()
+        else:
+            ids = [None] * n
+
+            def submitter():
+                for i in range(n):
+                    d = arrivals[i] - (time.perf_counter() - t0)
+                    if d > 0:
+                        time.sleep(d)
+                    ids[i] = submit(i)
+
+            th = threading.Thread(target=submitter)
+            th.start()
+            for i in range(n):
+                while ids[i] is None:
+                    time.sleep(0.0005)
+                finish(i, ids[i])
+            th.join()
         t_end = time.perf_counter()
-        th.join()
         clocks = clocks_stop(clk)
         st = srv.stats()
         srv.close()
@@ -1001,20 +1037,48 @@ def run_serving(args) -> int:
         out[arm] = {"storage": storage, "max_active": max_active, "completed": st["completed"],
                     "failed": st["failed"], "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
                     "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
-                    "throughput_per_s": st["completed"] / (t_end - t_start[0]),
-                    "makespan_s": t_end - t_start[0], "peak_active": st["peak_active"],
+                    "throughput_per_s": st["completed"] / (t_end - t0),
+                    "makespan_s": t_end - t0, "peak_active": st["peak_active"],
                     "mean_queue_ms": st["queue_ms"], "mean_load_ms": st["load_ms"], "mean_run_ms": st["run_ms"],
                     "peak_bytes": st["peak_bytes"], "by_kind": by_kind, "clocks": clocks}
+
+    def rel(a, b):
+        return float(np.linalg.norm(np.float64(a) - b) / max(np.linalg.norm(np.float64(b)), 1e-30))
+
+    # accuracy: each sampled reconstruction of the batched (FP16-storage) arm
+    # against the same request in the plain FP32 arm, and the first sampled
+    # 64^3 request of both arms against the FP64 oracle on its inputs
+    diffs = [rel(kept[("batched", i)], kept[("plain", i)]) for i in sample
+             if ("batched", i) in kept and ("plain", i) in kept]
+    accuracy = {"requests_compared": len(diffs),
+                "batched_vs_plain_rel_l2_max": max(diffs) if diffs else None,
+                "batched_vs_plain_rel_l2_median": float(np.median(diffs)) if diffs else None}
+    small = [i for i in sample if reqs[i][1] == "64^3"]
+    if small and args.fp64_oracle:
+        i = small[0]
+        _, nm, k, it = reqs[i]
+        g, nsub, sinos, _, _ = pool[nm]
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import gfo
+
+        gfo.build()
+        ref = gfo.Oracle(g.tuple(), "f64").recon(1, nsub=nsub, niter=it, dsino=sinos[k][0], norm=sinos[k][1])
+        accuracy["fp64_request"] = {"size": nm, "subsets": nsub, "iterations": int(it),
+                                    "plain_rel_l2_vs_fp64": rel(kept[("plain", i)], ref["img_d"]),
+                                    "batched_rel_l2_vs_fp64": rel(kept[("batched", i)], ref["img_d"])}
+    wl = (f"closed loop: {n} requests, {args.serve_closed} in flight at all times (capacity)" if closed else
+          f"Poisson request stream, {args.serve_rate:g} req/s for {args.serve_seconds:g} s")
     line = {"metric": "requests/s", "value": out["batched"]["throughput_per_s"], "unit": "req/s", "n_gpus": 1,
             "steps": n, "warmup": 0, "ms_per_step": out["batched"]["mean_ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 arithmetic",
             "data": "synthetic: seeded ellipsoid phantoms, gains U(0.85,1.15), Poisson",
-            "config": {"workload": f"Poisson request stream, {args.serve_rate:g} req/s for {args.serve_seconds:g} s, "
-                                   "sizes 64^3 / 96^3 / 128x128x159, 25% bare projections, "
-                                   "2-3 iterations, HBM budget 150 GB",
+            "config": {"workload": wl + ", sizes 64^3 / 96^3 / 128x128x159, 25% bare projections, "
+                                        "2-3 iterations, HBM budget 150 GB",
                        "requests": n, "subsets": {k: v[1] for k, v in SERVE_SIZES.items()},
                        "count_levels": {k: pool[k][4] for k in names}},
-            "arms": out}
+            "arms": out, "speedup_batched_vs_plain": out["batched"]["throughput_per_s"] /
+                                                     out["plain"]["throughput_per_s"],
+            "accuracy": accuracy}
     print(json.dumps(line))
     return 0
 
@@ -1037,6 +1101,9 @@ def main() -> int:
     ap.add_argument("--frames-geometry", default="preclinical", choices=["preclinical", "small"])
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-closed", type=int, default=0,
+                    help="serving: keep this many requests in flight (closed loop, capacity) instead of the stream")
+    ap.add_argument("--serve-requests", type=int, default=300, help="serving, closed loop: requests in all")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -290,7 +290,9 @@ class Recon:
 
     def close(self) -> None:
         if self.h:
-            lib().gf_recon_destroy(self.h)
+            # gf_destroy has already destroyed the reconstructions of a closed context
+            if self.ctx.h:
+                lib().gf_recon_destroy(self.h)
             self.h = ctypes.c_void_p()
 
     def __del__(self):
@@ -355,6 +357,16 @@ class Batch:
         h = ctypes.c_void_p()
         _ck(lib().gf_batch_create(len(self.recons), arr, ctypes.byref(h)))
         self.h = h
+
+    def set_fused(self, fused: bool = True) -> None:
+        """Fused groups: frames that match run each stage as one launch (gf_batch_set_fused)."""
+        _ck(lib().gf_batch_set_fused(self.h, int(fused)))
+
+    def groups(self) -> tuple:
+        """(units, largest group) as the batch stands now."""
+        n, big = ctypes.c_int32(), ctypes.c_int32()
+        _ck(lib().gf_batch_groups(self.h, ctypes.byref(n), ctypes.byref(big)))
+        return n.value, big.value
 
     def iterate(self, n: int = 1, graph: bool = True) -> None:
         _ck(lib().gf_batch_iterate(self.h, n, int(graph)))

@@ -1,17 +1,24 @@
 // gf_batch.cpp -- frames that advance together, replayed from a CUDA graph.
 //
 // Each frame is a loaded gf_recon with its own resident data, subset count
-// and stream.  One iteration of every frame is captured once: a fork event on
-// the batch's origin stream, each frame's sub-iteration kernels on its own
-// stream (a parallel branch of the graph, so frames overlap on the device),
-// a join event per frame back to the origin.  The graph is then launched once
-// per iteration.  Replay is exact because a sub-iteration's launches depend
-// only on the frame's (type, subset) cursor, which returns to the start
-// after a full iteration, and every buffer is updated in place.  The graph
-// holds each frame's launch parameters as captured (tile shapes, the mode-3
-// event count and buffers); a frame whose context was retuned or whose load
-// changed them since (gf_ctx::gen, gf_recon::gen) makes the next iterate
-// capture the graph again.
+// and stream.  The frames are split into units: with fusing on
+// (gf_batch_set_fused), mode-1 frames that share geometry, subset count,
+// storage, filters and tile shapes form fused groups of up to kMaxFrames,
+// whose sub-iterations run every stage as one launch over the group
+// (fused_subiteration); every other frame is a unit of its own.
+//
+// One iteration of every unit is captured once: a fork event on the batch's
+// origin stream, each unit's kernels on the stream of its first frame (a
+// parallel branch of the graph, so units overlap on the device), a join event
+// per unit back to the origin.  The graph is then launched once per
+// iteration.  Replay is exact because a sub-iteration's launches depend only
+// on the frames' (type, subset) cursors, which return to the start after a
+// full iteration, and every buffer is updated in place.  The graph holds the
+// launch parameters as captured (tile shapes, the mode-3 event count and
+// buffers, the grouping); a frame whose context was retuned or whose load
+// changed them since (gf_ctx::gen, gf_recon::gen), or a change of fusing,
+// makes the next iterate capture the graph again.
+#include <algorithm>
 #include <utility>
 #include <vector>
 
@@ -22,9 +29,11 @@ using namespace gf;
 struct gf_batch {
   std::vector<gf_recon*> frames;
   int device = 0;
+  bool fused = false;
+  std::vector<std::vector<int>> units;  // frame indices: a fused group, or one frame
   cudaStream_t origin = nullptr;
   cudaEvent_t fork = nullptr;
-  std::vector<cudaEvent_t> joins;
+  std::vector<cudaEvent_t> joins;  // one per frame (a unit uses its first frame's)
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
   std::vector<std::pair<int64_t, int64_t>> cap_gen;  // (context, reconstruction) generations at capture
@@ -45,6 +54,34 @@ static void drop_graph(gf_batch* b) {
   b->graph = nullptr;
 }
 
+// Units in frame order: with fusing, each frame joins the first open group
+// it can fuse with (fewer than kMaxFrames members), else opens a new one.
+static void make_units(gf_batch* b) {
+  b->units.clear();
+  for (int i = 0; i < (int)b->frames.size(); i++) {
+    bool placed = false;
+    if (b->fused && b->frames[i]->p.mode == 1) {
+      for (auto& u : b->units) {
+        if ((int)u.size() < kMaxFrames && fusable(b->frames[u[0]], b->frames[i])) {
+          u.push_back(i);
+          placed = true;
+          break;
+        }
+      }
+    }
+    if (!placed) b->units.push_back({i});
+  }
+}
+
+// One iteration of one unit on its first frame's stream.
+static gf_status unit_iteration(gf_batch* b, const std::vector<int>& u) {
+  if (u.size() == 1) return gf_recon_iterate(b->frames[u[0]], 1);
+  std::vector<gf_recon*> G;
+  for (int i : u) G.push_back(b->frames[i]);
+  for (int k = 0; k < G[0]->ctx->plan.nsub; k++) GF_TRY(fused_subiteration(G.data(), (int)G.size()));
+  return GF_OK;
+}
+
 extern "C" {
 
 gf_status gf_batch_create(int32_t n, gf_recon* const* frames, gf_batch** out) {
@@ -55,10 +92,13 @@ gf_status gf_batch_create(int32_t n, gf_recon* const* frames, gf_batch** out) {
     if (!frames[i]->loaded) return set_error(GF_ERR_STATE, "every frame must be loaded");
     if (frames[i]->ntypes == 0) return set_error(GF_ERR_STATE, "mode-0 frames have no iterations");
     if (frames[i]->ctx->device != frames[0]->ctx->device) return set_error(GF_ERR_ARG, "frames on different devices");
+    for (int j = 0; j < i; j++)
+      if (frames[j] == frames[i]) return set_error(GF_ERR_ARG, "a frame appears twice");
   }
   gf_batch* b = new gf_batch();
   b->frames.assign(frames, frames + n);
   b->device = frames[0]->ctx->device;
+  make_units(b);
   cudaSetDevice(b->device);
   cudaError_t e = cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
@@ -84,34 +124,80 @@ void gf_batch_destroy(gf_batch* b) {
   delete b;
 }
 
+gf_status gf_batch_set_fused(gf_batch* b, int32_t fused) {
+  if (!b) return set_error(GF_ERR_ARG, "null batch");
+  if ((fused != 0) == b->fused) return GF_OK;
+  GF_CK(cudaSetDevice(b->device));
+  GF_CK(cudaStreamSynchronize(b->origin));  // a queued replay may still use the graph
+  drop_graph(b);
+  b->fused = fused != 0;
+  make_units(b);
+  return GF_OK;
+}
+
+gf_status gf_batch_groups(gf_batch* b, int32_t* ngroups, int32_t* largest) {
+  if (!b) return set_error(GF_ERR_ARG, "null batch");
+  int n = 0, big = 0;
+  for (auto& u : b->units) {
+    n++;
+    big = std::max(big, (int)u.size());
+  }
+  if (ngroups) *ngroups = n;
+  if (largest) *largest = big;
+  return GF_OK;
+}
+
+}  // extern "C"
+
 static gf_status capture(gf_batch* b) {
   for (gf_recon* r : b->frames)
     if (r->cur_type != 0 || r->cur_sub != 0) return set_error(GF_ERR_STATE, "frames must stand at an iteration boundary");
+  // fusing may have been switched on before the frames matched (a retune):
+  // group them as they stand now
+  make_units(b);
   // the frames' streams must be idle before they join the capture
   for (gf_recon* r : b->frames) GF_CK(cudaStreamSynchronize(r->ctx->stream));
   std::vector<bool> prof(b->frames.size());
+  std::vector<gf_ctx*> ctxs;  // each context once: frames may share one
+  std::vector<int64_t> l0;
   for (size_t i = 0; i < b->frames.size(); i++) {
     prof[i] = b->frames[i]->prof;
     b->frames[i]->prof = false;  // no timing events inside the graph
+    gf_ctx* c = b->frames[i]->ctx;
+    if (std::find(ctxs.begin(), ctxs.end(), c) == ctxs.end()) {
+      ctxs.push_back(c);
+      l0.push_back(c->launches);
+    }
   }
   GF_CK(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed));
   gf_status st = GF_OK;
   cudaError_t e = cudaEventRecord(b->fork, b->origin);
-  for (size_t i = 0; i < b->frames.size() && e == cudaSuccess && st == GF_OK; i++) {
-    gf_recon* r = b->frames[i];
-    e = cudaStreamWaitEvent(r->ctx->stream, b->fork, 0);
+  for (size_t k = 0; k < b->units.size() && e == cudaSuccess && st == GF_OK; k++) {
+    const int first = b->units[k][0];
+    cudaStream_t s = b->frames[first]->ctx->stream;
+    e = cudaStreamWaitEvent(s, b->fork, 0);
     if (e != cudaSuccess) break;
-    const int per = r->ntypes * r->ctx->plan.nsub;
-    const int64_t l0 = r->ctx->launches;
-    for (int k = 0; k < per && st == GF_OK; k++) st = gf_recon_subiteration(r);
-    r->launches_per_iteration = r->ctx->launches - l0;
-    r->ctx->launches = l0;  // captured, not yet run
-    if (st == GF_OK) e = cudaEventRecord(b->joins[i], r->ctx->stream);
-    if (e == cudaSuccess && st == GF_OK) e = cudaStreamWaitEvent(b->origin, b->joins[i], 0);
+    st = unit_iteration(b, b->units[k]);
+    if (st == GF_OK) e = cudaEventRecord(b->joins[first], s);
+    if (e == cudaSuccess && st == GF_OK) e = cudaStreamWaitEvent(b->origin, b->joins[first], 0);
   }
   cudaGraph_t g = nullptr;
   cudaError_t e2 = cudaStreamEndCapture(b->origin, &g);
-  for (size_t i = 0; i < b->frames.size(); i++) b->frames[i]->prof = prof[i];
+  // a replay counts each context's captured launches once, through the
+  // first of its frames
+  for (size_t i = 0; i < b->frames.size(); i++) {
+    b->frames[i]->prof = prof[i];
+    b->frames[i]->launches_per_iteration = 0;
+  }
+  for (size_t k = 0; k < ctxs.size(); k++) {
+    for (gf_recon* r : b->frames) {
+      if (r->ctx == ctxs[k]) {
+        r->launches_per_iteration = ctxs[k]->launches - l0[k];
+        break;
+      }
+    }
+    ctxs[k]->launches = l0[k];  // captured, not yet run
+  }
   if (st != GF_OK) {
     if (g) cudaGraphDestroy(g);
     return st;
@@ -134,12 +220,30 @@ static gf_status capture(gf_batch* b) {
   return GF_OK;
 }
 
+extern "C" {
+
 gf_status gf_batch_iterate(gf_batch* b, int32_t n, int32_t use_graph) {
   if (!b || n < 0) return set_error(GF_ERR_ARG, "bad argument");
   GF_CK(cudaSetDevice(b->device));
   if (!use_graph) {
-    for (int it = 0; it < n; it++)
-      for (gf_recon* r : b->frames) GF_TRY(gf_recon_iterate(r, 1));
+    make_units(b);
+    for (int it = 0; it < n; it++) {
+      for (auto& u : b->units) {
+        // a fused group runs on its first frame's stream: it waits for the
+        // other frames' queued work, and their later work waits for it
+        cudaStream_t s0 = b->frames[u[0]]->ctx->stream;
+        for (size_t k = 1; k < u.size(); k++) {
+          GF_CK(cudaEventRecord(b->joins[u[k]], b->frames[u[k]]->ctx->stream));
+          GF_CK(cudaStreamWaitEvent(s0, b->joins[u[k]], 0));
+        }
+        GF_TRY(unit_iteration(b, u));
+        if (u.size() > 1) {
+          GF_CK(cudaEventRecord(b->joins[u[0]], s0));
+          for (size_t k = 1; k < u.size(); k++)
+            GF_CK(cudaStreamWaitEvent(b->frames[u[k]]->ctx->stream, b->joins[u[0]], 0));
+        }
+      }
+    }
     return GF_OK;
   }
   if (b->exec && stale(b)) {

@@ -126,7 +126,7 @@ __device__ __forceinline__ void voxel_views_fast(float2 (&acc)[Q], const float2*
 template <int Q, int NCH>
 __device__ __forceinline__ void voxel_window_fast(float2 (&acc)[Q], const float2* rv, float2 be2, float t,
                                                   float zlo) {
-  constexpr int W = NCH + 1;
+  constexpr int W = NCH + 1;  // bp_fast_pads (gf_plan.cpp) sizes the sentinel rows for this window
   if constexpr (W >= Q) {
     voxel_views_fast<Q, 0, Q - 1>(acc, rv, be2);
   } else {
@@ -141,6 +141,14 @@ __device__ __forceinline__ void voxel_window_fast(float2 (&acc)[Q], const float2
     }
   }
 }
+
+// Row chunks of FP32 pairs loaded during the previous view (the rest load
+// while staging), per back-projector form.
+#ifndef GF_BP_VIEW_PF32
+#define GF_BP_VIEW_PF32 4
+#endif
+template <bool FAST>
+constexpr int bp_pf32 = FAST ? GF_BP_VIEW_PF32 : 3;
 
 // One segment's views with its row chunk count NCH fixed at compile time, so
 // the staging issues exactly the chunks the segment's rows occupy.
@@ -159,7 +167,7 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
   // than the exposed loads cost (1.294 ms; all chunks prefetched at 72
   // registers, seven blocks: 1.336 ms; at 80 registers, six blocks: 1.343 ms).
   {
-    constexpr int PF = (sizeof(Pair) == 8 && NCH > 3) ? 3 : NCH;
+    constexpr int PF = (sizeof(Pair) == 8 && NCH > bp_pf32<FAST>) ? bp_pf32<FAST> : NCH;
     Pair c0[PF], c1[PF];
     auto load = [&](const int4& e) {
       const Pair* p0 = cc + e.x + sg.blk;
@@ -210,7 +218,8 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
 template <int Q, int STORE, bool FAST>
 __device__ __forceinline__ void bp_column(const BpArgs& a, int rmax) {
   using Pair = typename PairT<STORE>::type;
-  const Pair* cc = static_cast<const Pair*>(a.corrcal);
+  const BpFrame& F = a.fr[blockIdx.y];
+  const Pair* cc = static_cast<const Pair*>(F.corrcal);
   extern __shared__ __align__(16) unsigned char smraw[];
   const DevGeom& g = a.g;
   const int nwarps = blockDim.x >> 5;
@@ -268,8 +277,8 @@ __device__ __forceinline__ void bp_column(const BpArgs& a, int rmax) {
 #undef GF_SEG
     }
   }
-  float* no = a.numer + (size_t)colidx * g.nzp;
-  float* dO = a.denom + (size_t)colidx * g.nzp;
+  float* no = F.numer + (size_t)colidx * g.nzp;
+  float* dO = F.denom + (size_t)colidx * g.nzp;
 #pragma unroll
   for (int q = 0; q < Q; q++) {
     const int iz = lane + 32 * q;
@@ -322,7 +331,10 @@ cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st) {
   const int Q = a.g.nzp / 32;
   if (a.fast && (a.pad_lo < 0 || a.rbuf < a.pad_lo + a.g.nzs + 2)) return cudaErrorInvalidValue;
   const int rmax = a.fast ? a.rbuf : a.g.nzs + 2;
-  dim3 grid((a.g.res * a.g.res + warps - 1) / warps);
+  if (a.nfr < 0 || a.nfr > kMaxFrames) return cudaErrorInvalidValue;
+  for (int f = 0; f < (a.nfr > 1 ? a.nfr : 1); f++)
+    if (!a.fr[f].corrcal || !a.fr[f].numer || !a.fr[f].denom) return cudaErrorInvalidValue;
+  dim3 grid((a.g.res * a.g.res + warps - 1) / warps, a.nfr > 1 ? a.nfr : 1);
   size_t smem = (size_t)warps * (a.na * sizeof(int4) + rmax * sizeof(float2));
   void (*k)(BpArgs, int) = nullptr;
   switch (a.storage * 16 + Q) {

@@ -108,7 +108,8 @@ FpArgs gf_ctx::fp_args(int subset, const float* img_zfast) const {
   FpArgs a{};
   a.g = dg;
   a.subset = subset;
-  a.img = img_zfast;
+  a.nfr = 1;
+  a.fr[0].img = img_zfast;
   a.runs = d_runs;
   a.nruns = (int)fps.runs.size();
   a.padl = fps.padl;
@@ -122,9 +123,10 @@ BpArgs gf_ctx::bp_args(int subset, const void* cc, float* numer, float* denom, i
   b.g = dg;
   b.subset = subset;
   b.na = plan.sub_nang[subset];
-  b.corrcal = cc;
-  b.numer = numer;
-  b.denom = denom;
+  b.nfr = 1;
+  b.fr[0].corrcal = cc;
+  b.fr[0].numer = numer;
+  b.fr[0].denom = denom;
   b.storage = storage;
   b.fast = bp_form == GF_BP_PER_VIEW ? 1 : 0;
   b.pad_lo = bpp.pad_lo;
@@ -307,6 +309,8 @@ gf_status gf_create(const gf_geometry* g, int32_t nsubsets, int32_t device, gf_c
 void gf_destroy(gf_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
+  // reconstructions still open on this context go first: they free on its stream
+  while (!c->recons.empty()) gf_recon_destroy(c->recons.back());
   // wait for the context's work, then return its memory on a stream of the
   // library's own, so a caller's stream set by gf_set_stream is not needed
   if (c->stream) cudaStreamSynchronize(c->stream);
@@ -451,7 +455,7 @@ gf_status gf_forward_project(gf_ctx* c, const float* d_image, int32_t subset, fl
   GF_TRY(c->ensure_scratch());
   GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_image, c->s_img, c->stream));
   FpArgs a = c->fp_args(subset, c->s_img);
-  a.proj_full = d_proj;
+  a.fr[0].proj_full = d_proj;
   GF_LAUNCH(c, launch_fp(a, c->fps, c->stream));
   return GF_OK;
 }

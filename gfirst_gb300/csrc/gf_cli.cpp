@@ -15,9 +15,11 @@
 //                      event (gf_read_vlor_endpoints) instead of int32 bins
 //   --storage f32|f16|bf16   element type of the per-subset ratio sinogram
 //                            (arithmetic stays FP32; default f32)
-//   --image-storage f32|f16|bf16   element type of the doubles image between
-//                                  sub-iterations (mode 1 only; default f32)
+//   --image-storage f32|f16|bf16   element type of the reconstructed images
+//                                  between sub-iterations (default f32)
 //   --tune             pick the projectors' tile shapes by timing first
+//   --bp-form view|voxel   the back projector's axial interpolation for the
+//                          doubles image (gf_set_bp_form; default view)
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -33,7 +35,8 @@ static int usage() {
   printf("3 Inputs --> Reconstruction Doubles & Triples [Input = Sinog_Doubles + Sinog_Triples + Sinog_Normalization] \n");
   printf("4 Inputs --> VLOR reconstruction [Input = Sinog_Doubles + Sinog_Triples + Sinog_Normalization + Vlor_file] \n");
   printf("options: --geometry res,nzs,nrad,nang,span,nseg,pitch,diam,fov --subsets S --iterations N "
-         "--write-every K --device D --vlor-endpoints --storage f32|f16|bf16 --image-storage f32|f16|bf16 --tune\n");
+         "--write-every K --device D --vlor-endpoints --storage f32|f16|bf16 --image-storage f32|f16|bf16 --tune "
+         "--bp-form view|voxel\n");
   return 0;
 }
 
@@ -47,6 +50,7 @@ int main(int argc, char** argv) {
   gf_geometry_reference(&g);
   int nsub = 1, niter = -1, every = 20, device = 0;
   bool vlor_endpoints = false, tune = false;
+  int bp_form = GF_BP_PER_VIEW;
   int storage = GF_STORE_F32, image_storage = GF_STORE_F32;
   std::vector<std::string> files;
   for (int i = 1; i < argc; i++) {
@@ -77,6 +81,14 @@ int main(int argc, char** argv) {
       vlor_endpoints = true;
     } else if (a == "--tune") {
       tune = true;
+    } else if (a == "--bp-form") {
+      const std::string v = val("--bp-form");
+      if (v == "view") bp_form = GF_BP_PER_VIEW;
+      else if (v == "voxel") bp_form = GF_BP_PER_VOXEL;
+      else {
+        fprintf(stderr, "gfirst: --bp-form wants view or voxel\n");
+        return 2;
+      }
     } else if (a == "--storage" || a == "--image-storage") {
       const std::string v = val(a.c_str());
       int* dst = a == "--storage" ? &storage : &image_storage;
@@ -100,6 +112,7 @@ int main(int argc, char** argv) {
   if (st != GF_OK) return die("geometry", st);
   gf_ctx* ctx = nullptr;
   if ((st = gf_create(&g, nsub, device, &ctx)) != GF_OK) return die("gf_create", st);
+  if ((st = gf_set_bp_form(ctx, bp_form)) != GF_OK) return die("gf_set_bp_form", st);
   gf_recon_params p;
   gf_recon_defaults(mode, &p);
   if (niter >= 0) p.niter = niter;

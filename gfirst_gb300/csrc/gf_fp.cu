@@ -33,6 +33,7 @@ __global__ void __launch_bounds__(512) fp_kernel(const FpArgs a) {
   float* col = reinterpret_cast<float*>(wts + lc);           // [lc][cw]
 
   const DevGeom& g = a.g;
+  const FpFrame& F = a.fr[blockIdx.z];
   const int ird = blockIdx.x, tl = blockIdx.y;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int theta = subset_angle(g, a.subset, tl);
@@ -78,8 +79,8 @@ __global__ void __launch_bounds__(512) fp_kernel(const FpArgs a) {
       if (z < NZS) {
         const int4 o = offs[l];
         const float2 w = wts[l];
-        const float v00 = __ldg(a.img + o.x + z), v10 = __ldg(a.img + o.y + z);
-        const float v01 = __ldg(a.img + o.z + z), v11 = __ldg(a.img + o.w + z);
+        const float v00 = __ldg(F.img + o.x + z), v10 = __ldg(F.img + o.y + z);
+        const float v01 = __ldg(F.img + o.z + z), v11 = __ldg(F.img + o.w + z);
         col[l * cw + a.padl + z] = lerp_rn(lerp_rn(v00, v10, w.x), lerp_rn(v01, v11, w.x), w.y);
       }
     }
@@ -122,15 +123,15 @@ __global__ void __launch_bounds__(512) fp_kernel(const FpArgs a) {
       const float proj = acc[j];
       if (FULL) {
         const size_t lor = ((size_t)(iz0 - sg.zmin) + sg.acc) * ((size_t)g.nrad * g.nang) + (size_t)theta * g.nrad + ird;
-        a.proj_full[lor] = proj;
+        F.proj_full[lor] = proj;
       }
       if (RATIO) {
         const size_t o = base + sg.blk + 1 + (iz0 - sg.zmin);
-        const float2 db = a.dbg[o];
+        const float2 db = F.dbg[o];
         const float s = __fadd_rn(proj, db.y);
         const float corr = (s >= 0.01f) ? __fdiv_rn(db.x, s) : -1000.f;
-        Pair* cc_out = static_cast<Pair*>(a.corrcal);
-        const Pair cc = pair_from<Pair>(make_float2(corr, a.cal[o]));
+        Pair* cc_out = static_cast<Pair*>(F.corrcal);
+        const Pair cc = pair_from<Pair>(make_float2(corr, F.cal[o]));
         cc_out[o] = cc;
         if (j == 0 && (run.w & 1)) cc_out[o - 1] = (run.x == 0) ? cc : pair_from<Pair>(sentinel);
         if (j == run.z - 1 && (run.w & 2)) cc_out[o + 1] = (run.x == 0) ? cc : pair_from<Pair>(sentinel);
@@ -146,16 +147,17 @@ static cudaError_t launch_fp_t(const FpArgs& a, const FpSchedule& s, cudaStream_
   cudaError_t e = allow_max_smem(k);
   if (e != cudaSuccess) return e;
   int na = (a.g.nang - a.subset + a.g.nsub - 1) / a.g.nsub;
-  dim3 grid(a.g.nrad, na);
+  dim3 grid(a.g.nrad, na, a.nfr > 1 ? a.nfr : 1);
   k<<<grid, s.nthreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
 template <int R>
 static cudaError_t launch_fp_r(const FpArgs& a, const FpSchedule& s, cudaStream_t st) {
-  if (!a.corrcal) return launch_fp_t<R, false, true, 0>(a, s, st);
+  if (!a.fr[0].corrcal) return launch_fp_t<R, false, true, 0>(a, s, st);
   switch (a.storage) {
-    case 0: return a.proj_full ? launch_fp_t<R, true, true, 0>(a, s, st) : launch_fp_t<R, true, false, 0>(a, s, st);
+    case 0:
+      return a.fr[0].proj_full ? launch_fp_t<R, true, true, 0>(a, s, st) : launch_fp_t<R, true, false, 0>(a, s, st);
     case 1: return launch_fp_t<R, true, false, 1>(a, s, st);
     case 2: return launch_fp_t<R, true, false, 2>(a, s, st);
     default: return cudaErrorInvalidValue;
@@ -163,8 +165,15 @@ static cudaError_t launch_fp_r(const FpArgs& a, const FpSchedule& s, cudaStream_
 }
 
 cudaError_t launch_fp(const FpArgs& a, const FpSchedule& s, cudaStream_t st) {
-  if (!a.corrcal && !a.proj_full) return cudaErrorInvalidValue;
-  if (a.corrcal && a.proj_full && a.storage != 0) return cudaErrorInvalidValue;
+  if (a.nfr < 0 || a.nfr > kMaxFrames) return cudaErrorInvalidValue;
+  // every frame of a launch has the outputs of frame 0 (one kernel variant)
+  for (int f = 0; f < (a.nfr > 1 ? a.nfr : 1); f++) {
+    const FpFrame& F = a.fr[f];
+    if (!F.img || (!F.corrcal && !F.proj_full)) return cudaErrorInvalidValue;
+    if (!F.corrcal != !a.fr[0].corrcal || !F.proj_full != !a.fr[0].proj_full) return cudaErrorInvalidValue;
+    if (F.corrcal && (!F.dbg || !F.cal)) return cudaErrorInvalidValue;
+  }
+  if (a.fr[0].corrcal && a.fr[0].proj_full && a.storage != 0) return cudaErrorInvalidValue;
   switch (s.R) {
     case 9: return launch_fp_r<9>(a, s, st);
     case 17: return launch_fp_r<17>(a, s, st);

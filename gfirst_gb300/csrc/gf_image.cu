@@ -10,7 +10,7 @@
 
 namespace gf {
 
-// Image elements: FP32, or FP16/BF16 storage of the doubles image in mode 1
+// Image elements: FP32, or FP16/BF16 storage of the reconstructed images
 // (every operation in FP32; a store rounds to nearest even).
 __device__ __forceinline__ float img_ld(const float* p) { return *p; }
 __device__ __forceinline__ float img_ld(const __half* p) { return __half2float(*p); }
@@ -24,13 +24,17 @@ __device__ __forceinline__ void img_st(__nv_bfloat16* p, float v) { *p = __float
 // only for 3 < x < RES-4 and border columns output the raw input.  With DIV
 // the input is the update ratio numer/denom (1 where denom < 0.001,
 // divVxVGPU, GFIRST_GPU_Kernels.cu:173-182), computed on the fly.
+// Grid z runs over (frame, 32-slice chunk): frame f's buffers are fr.fr[f].
 template <bool DIV, class T>
-__global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const T* __restrict__ in,
-                                                      const float* __restrict__ den, const Taps9 G,
-                                                      float* __restrict__ out) {
+__global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const ImgFrames fr, const Taps9 G) {
   __shared__ float S[16][16][32];
+  const int nzc = g.nzp / 32;
+  const int f = blockIdx.z / nzc;
+  const T* __restrict__ in = static_cast<const T*>(fr.fr[f].in);
+  const float* __restrict__ den = fr.fr[f].den;
+  float* __restrict__ out = fr.fr[f].out;
   const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int x0 = blockIdx.x * 8, y0 = blockIdx.y * 8, z = blockIdx.z * 32 + lane;
+  const int x0 = blockIdx.x * 8, y0 = blockIdx.y * 8, z = (blockIdx.z - f * nzc) * 32 + lane;
   const int RES = g.res, NZP = g.nzp;
   if (!DIV) {
 #pragma unroll 8
@@ -95,21 +99,32 @@ __global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const T* 
   }
 }
 
-cudaError_t launch_conv_xy(const DevGeom& g, const void* in, const float* den, const Taps9& t, float* out,
-                           cudaStream_t st, int in_store) {
-  dim3 grid((g.res + 7) / 8, (g.res + 7) / 8, g.nzp / 32);
-  if (den) {
+cudaError_t launch_conv_xy_frames(const DevGeom& g, const ImgFrames& f, int nfr, bool div, const Taps9& t,
+                                  cudaStream_t st, int in_store) {
+  if (nfr < 1 || nfr > kMaxFrames) return cudaErrorInvalidValue;
+  for (int k = 0; k < nfr; k++)
+    if (!f.fr[k].in || !f.fr[k].out || (div && !f.fr[k].den)) return cudaErrorInvalidValue;
+  dim3 grid((g.res + 7) / 8, (g.res + 7) / 8, (g.nzp / 32) * nfr);
+  if (div) {
     if (in_store != 0) return cudaErrorInvalidValue;
-    conv_xy_kernel<true, float><<<grid, 256, 0, st>>>(g, static_cast<const float*>(in), den, t, out);
+    conv_xy_kernel<true, float><<<grid, 256, 0, st>>>(g, f, t);
   } else if (in_store == 1) {
-    conv_xy_kernel<false, __half><<<grid, 256, 0, st>>>(g, static_cast<const __half*>(in), nullptr, t, out);
+    conv_xy_kernel<false, __half><<<grid, 256, 0, st>>>(g, f, t);
   } else if (in_store == 2) {
-    conv_xy_kernel<false, __nv_bfloat16><<<grid, 256, 0, st>>>(g, static_cast<const __nv_bfloat16*>(in), nullptr, t,
-                                                                out);
+    conv_xy_kernel<false, __nv_bfloat16><<<grid, 256, 0, st>>>(g, f, t);
   } else {
-    conv_xy_kernel<false, float><<<grid, 256, 0, st>>>(g, static_cast<const float*>(in), nullptr, t, out);
+    conv_xy_kernel<false, float><<<grid, 256, 0, st>>>(g, f, t);
   }
   return cudaGetLastError();
+}
+
+cudaError_t launch_conv_xy(const DevGeom& g, const void* in, const float* den, const Taps9& t, float* out,
+                           cudaStream_t st, int in_store) {
+  ImgFrames f{};
+  f.fr[0].in = in;
+  f.fr[0].den = den;
+  f.fr[0].out = out;
+  return launch_conv_xy_frames(g, f, 1, den != nullptr, t, st, in_store);
 }
 
 // ---- axial filter, gaussian_filterZ (GFIRST_CPU_Kernels.cpp:165-187) -------
@@ -137,9 +152,11 @@ __device__ __forceinline__ float zrule(const float* c, int ze, int K, int NZS, c
 // values as the reference's multiply-then-copy order requires.  Voxel 0's
 // factor (DENOM[0] in the reference) only reaches slice 0, which the edge
 // copy overwrites.
+// Grid y runs over frames: frame f's C is fr.fr[f].out, its image fr.fr[f].img.
 template <int Q, class T>
-__global__ void __launch_bounds__(256) zfilter_update_kernel(const DevGeom g, const float* __restrict__ C,
-                                                             const Taps5 t5, T* img) {
+__global__ void __launch_bounds__(256) zfilter_update_kernel(const DevGeom g, const ImgFrames fr, const Taps5 t5) {
+  const float* __restrict__ C = fr.fr[blockIdx.y].out;
+  T* img = static_cast<T*>(fr.fr[blockIdx.y].img);
   const int lane = threadIdx.x & 31;
   const int colidx = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (colidx >= g.res * g.res) return;  // whole warp
@@ -170,11 +187,11 @@ __global__ void __launch_bounds__(256) zfilter_update_kernel(const DevGeom g, co
 }
 
 template <class T>
-static cudaError_t zfilter_update_t(const DevGeom& g, const float* C, const Taps5& t5, T* img, cudaStream_t st) {
-  dim3 grid((g.res * g.res + 7) / 8);
+static cudaError_t zfilter_update_t(const DevGeom& g, const ImgFrames& f, int nfr, const Taps5& t5, cudaStream_t st) {
+  dim3 grid((g.res * g.res + 7) / 8, nfr);
   switch (g.nzp / 32) {
 #define GF_ZF(QQ) \
-  case QQ: zfilter_update_kernel<QQ, T><<<grid, 256, 0, st>>>(g, C, t5, img); break;
+  case QQ: zfilter_update_kernel<QQ, T><<<grid, 256, 0, st>>>(g, f, t5); break;
     GF_ZF(1) GF_ZF(2) GF_ZF(3) GF_ZF(4) GF_ZF(5) GF_ZF(6) GF_ZF(7) GF_ZF(8)
 #undef GF_ZF
     default: return cudaErrorInvalidValue;
@@ -182,14 +199,25 @@ static cudaError_t zfilter_update_t(const DevGeom& g, const float* C, const Taps
   return cudaGetLastError();
 }
 
-cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const Taps5& t5, void* img, cudaStream_t st,
-                                  int img_store) {
+cudaError_t launch_zfilter_update_frames(const DevGeom& g, const ImgFrames& f, int nfr, const Taps5& t5,
+                                         cudaStream_t st, int img_store) {
+  if (nfr < 1 || nfr > kMaxFrames) return cudaErrorInvalidValue;
+  for (int k = 0; k < nfr; k++)
+    if (!f.fr[k].out || !f.fr[k].img) return cudaErrorInvalidValue;
   switch (img_store) {
-    case 0: return zfilter_update_t(g, C, t5, static_cast<float*>(img), st);
-    case 1: return zfilter_update_t(g, C, t5, static_cast<__half*>(img), st);
-    case 2: return zfilter_update_t(g, C, t5, static_cast<__nv_bfloat16*>(img), st);
+    case 0: return zfilter_update_t<float>(g, f, nfr, t5, st);
+    case 1: return zfilter_update_t<__half>(g, f, nfr, t5, st);
+    case 2: return zfilter_update_t<__nv_bfloat16>(g, f, nfr, t5, st);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const Taps5& t5, void* img, cudaStream_t st,
+                                  int img_store) {
+  ImgFrames f{};
+  f.fr[0].out = const_cast<float*>(C);
+  f.fr[0].img = img;
+  return launch_zfilter_update_frames(g, f, 1, t5, st, img_store);
 }
 
 // The axial filter on its own (voxel 0 keeps the value already in `out`).
@@ -304,21 +332,29 @@ cudaError_t launch_cylinder(const DevGeom& g, float val, void* out, cudaStream_t
 }
 
 // max(0, max over the image), GFIRST.cu:515, 521.  d_max must hold 0 before.
-__global__ void max_nonneg_kernel(const DevGeom g, const float* __restrict__ img, float* d_max) {
+// A maximum is exact in any precision: the reference's host loop and this
+// reduction give the same float.
+template <class T>
+__global__ void max_nonneg_kernel(const DevGeom g, const T* __restrict__ img, float* d_max) {
   const size_t n = (size_t)g.res * g.res * g.nzp;
   float m = 0.f;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const float v = img[i];
+    const float v = img_ld(img + i);
     if (v > m) m = v;
   }
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(reinterpret_cast<int*>(d_max), __float_as_int(m));
 }
 
-cudaError_t launch_max_nonneg(const DevGeom& g, const float* img, float* d_max, cudaStream_t st) {
+cudaError_t launch_max_nonneg(const DevGeom& g, const void* img, float* d_max, cudaStream_t st, int store) {
   cudaError_t e = cudaMemsetAsync(d_max, 0, sizeof(float), st);
   if (e != cudaSuccess) return e;
-  max_nonneg_kernel<<<304, 256, 0, st>>>(g, img, d_max);
+  switch (store) {
+    case 0: max_nonneg_kernel<<<304, 256, 0, st>>>(g, static_cast<const float*>(img), d_max); break;
+    case 1: max_nonneg_kernel<<<304, 256, 0, st>>>(g, static_cast<const __half*>(img), d_max); break;
+    case 2: max_nonneg_kernel<<<304, 256, 0, st>>>(g, static_cast<const __nv_bfloat16*>(img), d_max); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
@@ -331,8 +367,9 @@ cudaError_t launch_max_nonneg(const DevGeom& g, const float* img, float* d_max, 
 // (the reference evaluates it in double) and the intensity difference is
 // scaled by 1/max_ref.
 constexpr int BL_T = 4, BL_H = 4;
-__global__ void __launch_bounds__(512) bilateral_kernel(const DevGeom g, const float* __restrict__ in,
-                                                        const float* __restrict__ ref,
+template <class T>
+__global__ void __launch_bounds__(512) bilateral_kernel(const DevGeom g, const T* __restrict__ in,
+                                                        const T* __restrict__ ref,
                                                         const float* __restrict__ d_max_ref, float max_ref_host,
                                                         int r, float neg_inv_ci, const float* __restrict__ gtab,
                                                         float* __restrict__ out) {
@@ -350,8 +387,8 @@ __global__ void __launch_bounds__(512) bilateral_kernel(const DevGeom g, const f
     float vr = 0.f, vi = 0.f;
     if (y >= 0 && y < RES && x >= 0 && x < RES && z >= 0 && z < NZS) {
       const size_t o = ((size_t)y * RES + x) * NZP + z;
-      vr = ref[o];
-      vi = in[o];
+      vr = img_ld(ref + o);
+      vi = img_ld(in + o);
     }
     Sr[yy][xx][zz] = vr;
     Si[yy][xx][zz] = vi;
@@ -388,27 +425,45 @@ __global__ void __launch_bounds__(512) bilateral_kernel(const DevGeom g, const f
   out[((size_t)y * RES + x) * NZP + z] = (z < NZS) ? res : 0.f;
 }
 
-cudaError_t launch_bilateral(const DevGeom& g, const float* in, const float* ref, const float* d_max_ref,
-                             float max_ref, int r, float sigmai, const float* gtab, float* out, cudaStream_t st) {
+cudaError_t launch_bilateral(const DevGeom& g, const void* in, const void* ref, const float* d_max_ref,
+                             float max_ref, int r, float sigmai, const float* gtab, float* out, cudaStream_t st,
+                             int store) {
   if (r < 0 || r > BL_H) return cudaErrorInvalidValue;
   const double ci = (2.0 * (double)sigmai) * (2.0 * (double)sigmai);
   const float neg_inv_ci = (float)(-1.0 / ci);
   dim3 grid((g.res + BL_T - 1) / BL_T, (g.res + BL_T - 1) / BL_T, g.nzp / 32);
-  bilateral_kernel<<<grid, 512, 0, st>>>(g, in, ref, d_max_ref, max_ref, r, neg_inv_ci, gtab, out);
+  switch (store) {
+#define GF_BL(S, T)                                                                                        \
+  case S:                                                                                                  \
+    bilateral_kernel<<<grid, 512, 0, st>>>(g, static_cast<const T*>(in), static_cast<const T*>(ref),     \
+                                           d_max_ref, max_ref, r, neg_inv_ci, gtab, out);                 \
+    break;
+    GF_BL(0, float) GF_BL(1, __half) GF_BL(2, __nv_bfloat16)
+#undef GF_BL
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
 // img2 = (1.0 - 0.1f)*img2 + 0.1f*filtered, GFIRST.cu:524 (double, as there).
-__global__ void blend_kernel(size_t n, float* img2, const float* __restrict__ filt) {
+template <class T>
+__global__ void blend_kernel(size_t n, T* img2, const float* __restrict__ filt) {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float fc = 0.1f;
-  img2[i] = (float)(__dadd_rn(__dmul_rn(1.0 - (double)fc, (double)img2[i]), (double)__fmul_rn(fc, filt[i])));
+  img_st(img2 + i,
+         (float)(__dadd_rn(__dmul_rn(1.0 - (double)fc, (double)img_ld(img2 + i)), (double)__fmul_rn(fc, filt[i]))));
 }
 
-cudaError_t launch_blend(const DevGeom& g, float* img2, const float* filt, cudaStream_t st) {
+cudaError_t launch_blend(const DevGeom& g, void* img2, const float* filt, cudaStream_t st, int store) {
   const size_t n = (size_t)g.res * g.res * g.nzp;
-  blend_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, img2, filt);
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  switch (store) {
+    case 0: blend_kernel<<<nb, 256, 0, st>>>(n, static_cast<float*>(img2), filt); break;
+    case 1: blend_kernel<<<nb, 256, 0, st>>>(n, static_cast<__half*>(img2), filt); break;
+    case 2: blend_kernel<<<nb, 256, 0, st>>>(n, static_cast<__nv_bfloat16*>(img2), filt); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

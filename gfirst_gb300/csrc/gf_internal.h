@@ -55,6 +55,7 @@ struct gf_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   std::vector<gf::DevBuf> owned;  // freed on destroy
+  std::vector<gf_recon*> recons;  // reconstructions still open on this context (destroyed with it)
   gf::DevSeg* d_seg = nullptr;
   float2* d_trig = nullptr;
   int2* d_rowmap = nullptr;
@@ -67,7 +68,9 @@ struct gf_ctx {
   // (the projectors' tile shapes, gf_tune); gf_batch recaptures on a change.
   int64_t gen = 0;
   int bp_warps = 4;      // back-projector warps (columns) per block (eight blocks per SM fit the register cap)
-  int bp_form = GF_BP_PER_VOXEL;  // back projector's axial interpolation (gf_set_bp_form)
+  // back projector's axial interpolation for doubles images and the operator
+  // entry point (gf_set_bp_form); triples images always use GF_BP_PER_VOXEL
+  int bp_form = GF_BP_PER_VIEW;
   gf::BpPads bpp;        // staged-row buffer of the per-view form
   float* s_img = nullptr;
   float* s_img2 = nullptr;
@@ -91,7 +94,9 @@ struct gf_recon {
   int ntypes = 1;
   bool loaded = false;
   std::vector<gf::DevBuf> owned;
-  float* img[2] = {nullptr, nullptr};  // z-fast images (doubles, triples), updated in place
+  void* img[2] = {nullptr, nullptr};  // z-fast images (doubles, triples), updated in place
+  // element type of image t: image_storage, except mode 1's unused triples image (FP32)
+  int store(int t) const { return (t == 0 || p.mode >= 2) ? p.image_storage : GF_STORE_F32; }
   float* psf = nullptr;
   float* numer = nullptr;
   float* denom = nullptr;
@@ -141,4 +146,17 @@ struct gf_recon {
   gf_status subiteration(int type, int subset);
   gf_status init_images();
   gf_status project_all(const float* img_zfast, float* proj_full);
+  void advance();  // moves the (type, subset) cursor past one sub-iteration
 };
+
+namespace gf {
+// Frames a fused group may hold together: mode 1, one device, the same
+// geometry and subset count, storage, filters, back-projector form and tile
+// shapes, so one launch per stage serves them all.
+bool fusable(const gf_recon* a, const gf_recon* b);
+// One sub-iteration of every frame of a fused group (all at the same
+// subset): the forward PSF, projection + ratio, back projection and update
+// are one launch each over the nfr <= kMaxFrames frames, on the first
+// frame's stream and with its tables.  Advances every frame's cursor.
+gf_status fused_subiteration(gf_recon* const* G, int nfr);
+}  // namespace gf

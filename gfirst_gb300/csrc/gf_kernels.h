@@ -18,28 +18,42 @@ template <> struct PairT<2> { using type = __nv_bfloat162; };
 struct Taps9 { float c[9]; };
 struct Taps5 { float c[5]; };
 
+// One launch may serve several frames of one geometry and subset (a fused
+// group of a batch): every per-frame buffer sits in a table of kMaxFrames
+// entries passed by value, the launch has one grid slice per frame, and a
+// block takes its frame's entry.  A single-frame launch fills entry 0.
+constexpr int kMaxFrames = 16;
+
 // ---- forward projector (gf_fp.cu) ----
-struct FpArgs {
-  DevGeom g;
-  int subset;
+struct FpFrame {
   const float* img;        // z-fast image (after the forward PSF)
-  const int4* runs;        // FpSchedule::runs as (seg, p0, n, pad)
-  int nruns, padl, cw, lc;
   const float2* dbg;       // subset layout (data*RES, max(bg*RES,0)); with corrcal
   const float* cal;        // subset layout normalization mask; with corrcal
   void* corrcal;           // subset layout (corr, calib) pairs output, or null
   float* proj_full;        // file-layout projection output, or null
+};
+struct FpArgs {
+  DevGeom g;
+  int subset;
+  const int4* runs;        // FpSchedule::runs as (seg, p0, n, pad)
+  int nruns, padl, cw, lc;
   int storage;             // corrcal pair type: 0 float2, 1 __half2, 2 __nv_bfloat162
+  int nfr;                 // frames in this launch (grid z); 0 is taken as 1
+  FpFrame fr[kMaxFrames];
 };
 cudaError_t launch_fp(const FpArgs& a, const FpSchedule& s, cudaStream_t st);
 
 // ---- back projector (gf_bp.cu) ----
-struct BpArgs {
-  DevGeom g;
-  int subset, na;          // na: angles in this subset
+struct BpFrame {
   const void* corrcal;     // subset layout (corr, calib) pairs
   float* numer;            // z-fast
   float* denom;            // z-fast
+};
+struct BpArgs {
+  DevGeom g;
+  int subset, na;          // na: angles in this subset
+  int nfr;                 // frames in this launch (grid y); 0 is taken as 1
+  BpFrame fr[kMaxFrames];
   int storage;             // corrcal pair type, as FpArgs::storage
   // Axial interpolation: 0 per voxel with the reference's rounding (the
   // oracle's sums bit for bit), 1 per view (BpPads; within 1e-5 of it).
@@ -68,19 +82,35 @@ inline cudaError_t allow_max_smem(K k) {
 cudaError_t launch_conv_xy(const DevGeom& g, const void* in, const float* den, const Taps9& t, float* out,
                            cudaStream_t st, int in_store = 0);
 // img *= axial_filter(C), then the edge-slice copy; in place.
-// img elements: in_store/img_store/out_store 0 FP32, 1 FP16, 2 BF16 (mode-1 doubles image)
+// img elements: in_store/img_store/out_store 0 FP32, 1 FP16, 2 BF16 (16-bit image storage)
 cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const Taps5& t5, void* img, cudaStream_t st,
                                   int img_store = 0);
+// The same two over nfr frames of one geometry in one launch each.
+struct ImgFrame {
+  const void* in;   // conv_xy input (image, or NUMER with den)
+  const float* den; // conv_xy: DENOM of the update ratio, or null
+  float* out;       // conv_xy output; the zfilter's C
+  void* img;        // zfilter_update: the image updated in place
+};
+struct ImgFrames {
+  ImgFrame fr[kMaxFrames];
+};
+cudaError_t launch_conv_xy_frames(const DevGeom& g, const ImgFrames& f, int nfr, bool div, const Taps9& t,
+                                  cudaStream_t st, int in_store = 0);
+cudaError_t launch_zfilter_update_frames(const DevGeom& g, const ImgFrames& f, int nfr, const Taps5& t5,
+                                         cudaStream_t st, int img_store = 0);
 // Axial filter alone, z-fast in/out (voxel 0 keeps out's value).
 cudaError_t launch_zfilter(const DevGeom& g, const float* C, const Taps5& t5, float* out, cudaStream_t st);
 cudaError_t launch_file_to_zfast(const DevGeom& g, const float* in, float* out, cudaStream_t st);
 cudaError_t launch_zfast_to_file(const DevGeom& g, const void* in, float scale, int mask, float* out,
                                  cudaStream_t st, int in_store = 0);
 cudaError_t launch_cylinder(const DevGeom& g, float val, void* out, cudaStream_t st, int out_store = 0);
-cudaError_t launch_max_nonneg(const DevGeom& g, const float* img, float* d_max, cudaStream_t st);
-cudaError_t launch_bilateral(const DevGeom& g, const float* in, const float* ref, const float* d_max_ref,
-                             float max_ref, int r, float sigmai, const float* gtab, float* out, cudaStream_t st);
-cudaError_t launch_blend(const DevGeom& g, float* img2, const float* filt, cudaStream_t st);
+// store: element type of the image arguments (0 FP32, 1 FP16, 2 BF16)
+cudaError_t launch_max_nonneg(const DevGeom& g, const void* img, float* d_max, cudaStream_t st, int store = 0);
+cudaError_t launch_bilateral(const DevGeom& g, const void* in, const void* ref, const float* d_max_ref,
+                             float max_ref, int r, float sigmai, const float* gtab, float* out, cudaStream_t st,
+                             int store = 0);
+cudaError_t launch_blend(const DevGeom& g, void* img2, const float* filt, cudaStream_t st, int store = 0);
 
 // ---- sinogram kernels (gf_sino.cu) ----
 // rowmap[row'] = (segment, plane) of a padded row, (-1,-1) for a pad row.

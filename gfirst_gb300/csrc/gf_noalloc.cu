@@ -102,13 +102,14 @@ extern "C" gf_status gf_forward_project_noalloc(const gf_geometry* gg, int32_t n
   FpArgs a{};
   a.g = dg;
   a.subset = subset;
-  a.img = img;
+  a.nfr = 1;
+  a.fr[0].img = img;
   a.runs = druns;
   a.nruns = (int)fps.runs.size();
   a.padl = fps.padl;
   a.cw = fps.cw;
   a.lc = fps.lc;
-  a.proj_full = d_proj;
+  a.fr[0].proj_full = d_proj;
   GF_CK(launch_fp(a, fps, st));
   return GF_OK;
 }

@@ -14,6 +14,7 @@
 // iteration -> type (doubles, triples) -> subset.  With nsub = 1 this is the
 // reference's loop.  The joint filter runs after the triples type's last
 // subset, i.e. once per iteration as in the reference.
+#include <algorithm>
 #include <cstring>
 
 #include "gf_internal.h"
@@ -63,7 +64,7 @@ void gf_recon::stage_end() {
 gf_status gf_recon::project_all(const float* img_zfast, float* proj_full) {
   for (int s = 0; s < ctx->plan.nsub; s++) {
     FpArgs a = ctx->fp_args(s, img_zfast);
-    a.proj_full = proj_full;
+    a.fr[0].proj_full = proj_full;
     GF_LAUNCH(ctx, launch_fp(a, ctx->fps, ctx->stream));
   }
   return GF_OK;
@@ -74,10 +75,10 @@ gf_status gf_recon::project_all(const float* img_zfast, float* proj_full) {
 gf_status gf_recon::init_images() {
   gf_ctx* c = ctx;
   cudaStream_t st = c->stream;
-  GF_LAUNCH(c, launch_cylinder(c->dg, 1.0f, img[0], st, p.image_storage));
-  GF_LAUNCH(c, launch_cylinder(c->dg, p.mode == 1 ? 0.0f : 1.0f, img[1], st));
+  GF_LAUNCH(c, launch_cylinder(c->dg, 1.0f, img[0], st, store(0)));
+  GF_LAUNCH(c, launch_cylinder(c->dg, p.mode == 1 ? 0.0f : 1.0f, img[1], st, store(1)));
   if (p.mode == 3) {
-    GF_LAUNCH(c, launch_conv_xy(c->dg, img[1], nullptr, g_fw, psf, st));
+    GF_LAUNCH(c, launch_conv_xy(c->dg, img[1], nullptr, g_fw, psf, st, store(1)));
     GF_TRY(project_all(psf, proj_t));
     GF_CK(cudaMemsetAsync(datos_v, 0, c->plan.ndata * sizeof(float), st));
   }
@@ -94,11 +95,11 @@ gf_status gf_recon::subiteration(int t, int s) {
   const int na = pl.sub_nang[s];
   const int64_t off = pl.sub_off[s];
   stage_begin(GF_STAGE_PSF);
-  GF_LAUNCH(c, launch_conv_xy(c->dg, img[t], nullptr, g_fw, psf, st, t == 0 ? p.image_storage : 0));
+  GF_LAUNCH(c, launch_conv_xy(c->dg, img[t], nullptr, g_fw, psf, st, store(t)));
   stage_end();
   FpArgs a = c->fp_args(s, psf);
   if (p.mode == 3 && t == 1) {
-    a.proj_full = proj_t;
+    a.fr[0].proj_full = proj_t;
     stage_begin(GF_STAGE_FP);
     GF_LAUNCH(c, launch_fp(a, c->fps, st));
     stage_end();
@@ -109,32 +110,101 @@ gf_status gf_recon::subiteration(int t, int s) {
                                      p.storage, st));
     stage_end();
   } else {
-    a.dbg = dbg[t] + off;
-    a.cal = cal + off;
-    a.corrcal = corrcal;
+    a.fr[0].dbg = dbg[t] + off;
+    a.fr[0].cal = cal + off;
+    a.fr[0].corrcal = corrcal;
     a.storage = p.storage;
     stage_begin(GF_STAGE_FP);
     GF_LAUNCH(c, launch_fp(a, c->fps, st));
     stage_end();
   }
   BpArgs b = c->bp_args(s, corrcal, numer, denom, p.storage);
+  // Triples data are mostly zero, and where a ratio of exactly 0 meets a
+  // sentinel row the gap rule (GFIRST_GPU_Kernels.cu:157) turns on whether an
+  // interpolation weight rounds to 0: the triples image follows the
+  // reference's per-voxel rounding, or it drifts by ~1e-3 from it.
+  if (t == 1) b.fast = 0;
   stage_begin(GF_STAGE_BP);
   GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
   stage_end();
   stage_begin(GF_STAGE_UPDATE);
   GF_LAUNCH(c, launch_conv_xy(c->dg, numer, denom, g_bw, ctmp, st));
-  GF_LAUNCH(c, launch_zfilter_update(c->dg, ctmp, g5, img[t], st, t == 0 ? p.image_storage : 0));
+  GF_LAUNCH(c, launch_zfilter_update(c->dg, ctmp, g5, img[t], st, store(t)));
   stage_end();
   if (t == 1 && s == pl.nsub - 1) {
     // GFIRST.cu:512-524: r=4, sigma3D=0.75, sigmaI=0.025, max_ref over the doubles image
     stage_begin(GF_STAGE_BILATERAL);
-    GF_LAUNCH(c, launch_max_nonneg(c->dg, img[0], d_max, st));
-    GF_LAUNCH(c, launch_bilateral(c->dg, img[1], img[0], d_max, 0.f, 4, 0.025f, c->d_gtab, filt, st));
-    GF_LAUNCH(c, launch_blend(c->dg, img[1], filt, st));
+    GF_LAUNCH(c, launch_max_nonneg(c->dg, img[0], d_max, st, store(0)));
+    GF_LAUNCH(c, launch_bilateral(c->dg, img[1], img[0], d_max, 0.f, 4, 0.025f, c->d_gtab, filt, st, store(0)));
+    GF_LAUNCH(c, launch_blend(c->dg, img[1], filt, st, store(1)));
     stage_end();
   }
   return GF_OK;
 }
+
+void gf_recon::advance() {
+  subs_done++;
+  if (++cur_sub == ctx->plan.nsub) {
+    cur_sub = 0;
+    if (++cur_type == ntypes) {
+      cur_type = 0;
+      iters_done++;
+    }
+  }
+}
+
+namespace gf {
+
+bool fusable(const gf_recon* a, const gf_recon* b) {
+  const gf_ctx* x = a->ctx;
+  const gf_ctx* y = b->ctx;
+  const Geom& g = x->plan.g;
+  const Geom& h = y->plan.g;
+  const bool same_geom = g.res == h.res && g.nzs == h.nzs && g.nrad == h.nrad && g.nang == h.nang &&
+                         g.span == h.span && g.nseg == h.nseg && g.pitch == h.pitch && g.diam == h.diam &&
+                         g.fov == h.fov;
+  return a->p.mode == 1 && b->p.mode == 1 && a->loaded && b->loaded && x->device == y->device && same_geom &&
+         x->plan.nsub == y->plan.nsub && a->p.storage == b->p.storage &&
+         a->p.image_storage == b->p.image_storage && a->p.psf_fw == b->p.psf_fw && a->p.psf_bw == b->p.psf_bw &&
+         x->bp_form == y->bp_form && x->bp_warps == y->bp_warps && x->fps.R == y->fps.R && x->fps.lc == y->fps.lc;
+}
+
+gf_status fused_subiteration(gf_recon* const* G, int nfr) {
+  if (nfr < 1 || nfr > kMaxFrames) return set_error(GF_ERR_ARG, "fused group size out of range");
+  gf_recon* r0 = G[0];
+  gf_ctx* c = r0->ctx;
+  const Plan& pl = c->plan;
+  cudaStream_t st = c->stream;
+  const int s = r0->cur_sub;
+  for (int k = 1; k < nfr; k++)
+    if (G[k]->cur_sub != s || G[k]->cur_type != 0 || !fusable(r0, G[k]))
+      return set_error(GF_ERR_STATE, "frames of a fused group must match and stand at the same subset");
+  const int64_t off = pl.sub_off[s];
+  ImgFrames f{};
+  for (int k = 0; k < nfr; k++) {
+    f.fr[k].in = G[k]->img[0];
+    f.fr[k].out = G[k]->psf;
+  }
+  GF_LAUNCH(c, launch_conv_xy_frames(c->dg, f, nfr, false, r0->g_fw, st, r0->store(0)));
+  FpArgs a = c->fp_args(s, nullptr);
+  a.nfr = nfr;
+  a.storage = r0->p.storage;
+  for (int k = 0; k < nfr; k++)
+    a.fr[k] = FpFrame{G[k]->psf, G[k]->dbg[0] + off, G[k]->cal + off, G[k]->corrcal, nullptr};
+  GF_LAUNCH(c, launch_fp(a, c->fps, st));
+  BpArgs b = c->bp_args(s, r0->corrcal, r0->numer, r0->denom, r0->p.storage);
+  b.nfr = nfr;
+  for (int k = 0; k < nfr; k++) b.fr[k] = BpFrame{G[k]->corrcal, G[k]->numer, G[k]->denom};
+  GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
+  ImgFrames u{};
+  for (int k = 0; k < nfr; k++) u.fr[k] = ImgFrame{G[k]->numer, G[k]->denom, G[k]->ctmp, G[k]->img[0]};
+  GF_LAUNCH(c, launch_conv_xy_frames(c->dg, u, nfr, true, r0->g_bw, st));
+  GF_LAUNCH(c, launch_zfilter_update_frames(c->dg, u, nfr, r0->g5, st, r0->store(0)));
+  for (int k = 0; k < nfr; k++) G[k]->advance();
+  return GF_OK;
+}
+
+}  // namespace gf
 
 extern "C" {
 
@@ -161,11 +231,12 @@ gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out)
   if (prm->storage < GF_STORE_F32 || prm->storage > GF_STORE_BF16) return set_error(GF_ERR_ARG, "unknown storage");
   if (prm->image_storage < GF_STORE_F32 || prm->image_storage > GF_STORE_BF16)
     return set_error(GF_ERR_ARG, "unknown image storage");
-  if (prm->image_storage != GF_STORE_F32 && prm->mode != 1)
-    return set_error(GF_ERR_ARG, "16-bit image storage is for mode 1 only");
+  if (prm->image_storage != GF_STORE_F32 && prm->mode == 0)
+    return set_error(GF_ERR_ARG, "mode 0 has no reconstructed image");
   GF_CK(cudaSetDevice(c->device));
   gf_recon* r = new gf_recon();
   r->ctx = c;
+  c->recons.push_back(r);
   r->p = *prm;
   r->ntypes = prm->mode == 0 ? 0 : (prm->mode == 1 ? 1 : 2);
   const Plan& pl = c->plan;
@@ -176,12 +247,14 @@ gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out)
   gf_status st;
 #define ALLOC(ptr, n) \
   if ((st = r->alloc_t((size_t)(n), &(ptr))) != GF_OK) return fail(st)
-  // the doubles image: FP32, or 16-bit elements (mode 1, image_storage)
-  if ((st = r->alloc((size_t)pl.nvoxp * (prm->image_storage == GF_STORE_F32 ? 4 : 2), (void**)&r->img[0])) != GF_OK)
+  // the images: FP32, or 16-bit elements (image_storage; the triples image of
+  // modes 2-3 too, mode 1's unused triples image stays FP32)
+  if ((st = r->alloc((size_t)pl.nvoxp * (r->store(0) == GF_STORE_F32 ? 4 : 2), (void**)&r->img[0])) != GF_OK)
     return fail(st);
   ALLOC(r->proj_ref, pl.ndata);
   if (prm->mode >= 1) {
-    ALLOC(r->img[1], pl.nvoxp);
+    if ((st = r->alloc((size_t)pl.nvoxp * (r->store(1) == GF_STORE_F32 ? 4 : 2), (void**)&r->img[1])) != GF_OK)
+      return fail(st);
     ALLOC(r->psf, pl.nvoxp);
     ALLOC(r->numer, pl.nvoxp);
     ALLOC(r->denom, pl.nvoxp);
@@ -212,6 +285,8 @@ gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out)
 
 void gf_recon_destroy(gf_recon* r) {
   if (!r) return;
+  auto& rs = r->ctx->recons;
+  rs.erase(std::remove(rs.begin(), rs.end(), r), rs.end());
   for (auto& b : r->owned) cudaFreeAsync(b.p, r->ctx->stream);
   cudaStreamSynchronize(r->ctx->stream);
   for (auto& e : r->evs) {
@@ -246,8 +321,10 @@ static gf_status load_impl(gf_recon* r, const float* h_image, const float* h_dsi
   gf_status s;
   if (mode == 0) {
     if ((s = ck(cudaMemcpyAsync(stage, h_image, pl.nvox * sizeof(float), cudaMemcpyHostToDevice, st), "upload image")) != GF_OK) return done(s);
-    if ((s = ck(launch_file_to_zfast(c->dg, stage, r->img[0], st), "layout")) != GF_OK) return done(s);
-    if ((s = r->project_all(r->img[0], r->proj_ref)) != GF_OK) return done(s);
+    // mode 0: an FP32 image (image_storage is refused for it)
+    float* img0 = static_cast<float*>(r->img[0]);
+    if ((s = ck(launch_file_to_zfast(c->dg, stage, img0, st), "layout")) != GF_OK) return done(s);
+    if ((s = r->project_all(img0, r->proj_ref)) != GF_OK) return done(s);
     r->loaded = true;
     return done(GF_OK);
   }
@@ -333,14 +410,7 @@ gf_status gf_recon_subiteration(gf_recon* r) {
   if (!r->loaded) return set_error(GF_ERR_STATE, "gf_recon_load has not run");
   if (r->ntypes == 0) return set_error(GF_ERR_STATE, "mode 0 has no iterations");
   GF_TRY(r->subiteration(r->cur_type, r->cur_sub));
-  r->subs_done++;
-  if (++r->cur_sub == r->ctx->plan.nsub) {
-    r->cur_sub = 0;
-    if (++r->cur_type == r->ntypes) {
-      r->cur_type = 0;
-      r->iters_done++;
-    }
-  }
+  r->advance();
   return GF_OK;
 }
 
@@ -394,8 +464,7 @@ gf_status gf_recon_get_image(gf_recon* r, int32_t type, int32_t scaled, float* h
   float* tmp = nullptr;
   GF_CK(cudaMallocAsync(&tmp, pl.nvox * sizeof(float), c->stream));
   const float scale = type == 0 ? r->p.scale_d : r->p.scale_t;
-  cudaError_t e = launch_zfast_to_file(c->dg, r->img[type], scale, scaled ? 1 : 0, tmp, c->stream,
-                                       type == 0 ? r->p.image_storage : 0);
+  cudaError_t e = launch_zfast_to_file(c->dg, r->img[type], scale, scaled ? 1 : 0, tmp, c->stream, r->store(type));
   if (e == cudaSuccess) e = cudaMemcpyAsync(h_out, tmp, pl.nvox * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
   cudaFreeAsync(tmp, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

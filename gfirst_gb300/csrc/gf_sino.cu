@@ -30,74 +30,95 @@ __device__ __forceinline__ bool resolve_row(const DevGeom& g, int2 m, int* seg, 
   return true;
 }
 
-// All-subset element index -> (subset-local angle, angle, radial, row).
-__device__ __forceinline__ void decode_all(const DevGeom& g, size_t i, int* theta, int* r, int* p) {
-  *p = (int)(i % g.PS);
-  const size_t q = i / g.PS;
-  *r = (int)(q % g.nrad);
-  const int idx = (int)(q / g.nrad);  // angle rank within the concatenated subsets
-  // subsets are stored in order; subset s holds angles s, s+nsub, ...
-  int s = 0, base = 0;
-  for (;;) {
-    const int na = (g.nang - s + g.nsub - 1) / g.nsub;
-    if (idx < base + na) {
-      *theta = s + (idx - base) * g.nsub;
-      return;
-    }
-    base += na;
-    s++;
-  }
+// Rank of angle theta in the all-subset layout: subsets are stored in order,
+// subset s = theta % nsub holding angles s, s + nsub, ...; the first
+// nang % nsub subsets hold one angle more than the others.
+__device__ __forceinline__ int angle_rank(const DevGeom& g, int theta) {
+  const int s = theta % g.nsub, l = theta / g.nsub;
+  const int q = g.nang / g.nsub, rem = g.nang % g.nsub;
+  return s * q + min(s, rem) + l;
 }
+
+// The static subset layouts are a transpose of the file layout: for one
+// angle, file element (plane, radial) goes to (radial, padded row).  A block
+// moves a tile of 32 radial bins x 32 padded rows through shared memory, so
+// both the file reads (along radial bins) and the layout writes (along rows)
+// are whole 128-byte lines.
 
 // (data*RES, max(bg*RES, 0)) for every subset, from the parsed file
 // (2*NDATA floats: prompts then background).  GFIRST.cu:224-226, 423.
-__global__ void build_dbg_kernel(const DevGeom g, const int2* __restrict__ rowmap, const float* __restrict__ sino2,
-                                 float2* __restrict__ dbg, size_t n, size_t ndata) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int theta, r, p, seg, plane;
-  decode_all(g, i, &theta, &r, &p);
-  float2 v = make_float2(0.f, 0.f);
-  const int2 m = rowmap[p];
-  if (m.x >= 0 && m.y >= 0) {
-    seg = m.x;
-    plane = m.y;
-    const size_t lor = file_lor(g, seg, plane, theta, r);
-    const float res = (float)g.res;
-    const float bg = __fmul_rn(res, sino2[ndata + lor]);
-    v = make_float2(__fmul_rn(res, sino2[lor]), ((double)bg < 0.) ? 0.f : bg);
+// Pad rows hold (0, 0).
+__global__ void __launch_bounds__(256) build_dbg_kernel(const DevGeom g, const int2* __restrict__ rowmap,
+                                                        const float* __restrict__ sino2, float2* __restrict__ dbg,
+                                                        size_t ndata) {
+  __shared__ float2 tile[32][33];
+  const int r0 = blockIdx.x * 32, p0 = blockIdx.y * 32, theta = blockIdx.z;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const float res = (float)g.res;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int p = p0 + ty + 8 * k, r = r0 + tx;
+    float2 v = make_float2(0.f, 0.f);
+    if (p < g.PS && r < g.nrad) {
+      const int2 m = rowmap[p];
+      if (m.x >= 0 && m.y >= 0) {
+        const size_t lor = file_lor(g, m.x, m.y, theta, r);
+        const float bg = __fmul_rn(res, sino2[ndata + lor]);
+        v = make_float2(__fmul_rn(res, sino2[lor]), ((double)bg < 0.) ? 0.f : bg);
+      }
+    }
+    tile[ty + 8 * k][tx] = v;
   }
-  dbg[i] = v;
+  __syncthreads();
+  const size_t base = (size_t)angle_rank(g, theta) * g.nrad;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int r = r0 + ty + 8 * k, p = p0 + tx;
+    if (r < g.nrad && p < g.PS) dbg[(base + r) * g.PS + p] = tile[tx][ty + 8 * k];
+  }
 }
 
 cudaError_t launch_build_dbg(const DevGeom& g, const int2* rowmap, const float* sino2, float2* dbg,
                              cudaStream_t st) {
-  const size_t n = (size_t)g.nang * g.nrad * g.PS;
   const size_t ndata = (size_t)g.P * g.nang * g.nrad;
-  build_dbg_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, rowmap, sino2, dbg, n, ndata);
+  const dim3 grid((g.nrad + 31) / 32, (g.PS + 31) / 32, g.nang);
+  build_dbg_kernel<<<grid, dim3(32, 8), 0, st>>>(g, rowmap, sino2, dbg, ndata);
   return cudaGetLastError();
 }
 
 // Normalization mask per subset element, GFIRST.cu:447, 453-458: 1 where
-// proj_blank > 0.01 and blank > 0.01, else -1000; oblique pad rows -1000.
-__global__ void build_cal_kernel(const DevGeom g, const int2* __restrict__ rowmap, const float* __restrict__ proj_ref,
-                                 const float* __restrict__ norm, float* __restrict__ cal, size_t n) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int theta, r, p, seg, plane;
-  decode_all(g, i, &theta, &r, &p);
-  float v = -1000.f;
-  if (resolve_row(g, rowmap[p], &seg, &plane)) {
-    const size_t lor = file_lor(g, seg, plane, theta, r);
-    v = ((double)proj_ref[lor] > 0.01 && (double)norm[lor] > 0.01) ? 1.0f : -1000.f;
+// proj_blank > 0.01 and blank > 0.01, else -1000; oblique pad rows -1000,
+// segment 0's pad rows repeat its first/last plane.
+__global__ void __launch_bounds__(256) build_cal_kernel(const DevGeom g, const int2* __restrict__ rowmap,
+                                                        const float* __restrict__ proj_ref,
+                                                        const float* __restrict__ norm, float* __restrict__ cal) {
+  __shared__ float tile[32][33];
+  const int r0 = blockIdx.x * 32, p0 = blockIdx.y * 32, theta = blockIdx.z;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int p = p0 + ty + 8 * k, r = r0 + tx;
+    float v = -1000.f;
+    int seg, plane;
+    if (p < g.PS && r < g.nrad && resolve_row(g, rowmap[p], &seg, &plane)) {
+      const size_t lor = file_lor(g, seg, plane, theta, r);
+      v = ((double)proj_ref[lor] > 0.01 && (double)norm[lor] > 0.01) ? 1.0f : -1000.f;
+    }
+    tile[ty + 8 * k][tx] = v;
   }
-  cal[i] = v;
+  __syncthreads();
+  const size_t base = (size_t)angle_rank(g, theta) * g.nrad;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int r = r0 + ty + 8 * k, p = p0 + tx;
+    if (r < g.nrad && p < g.PS) cal[(base + r) * g.PS + p] = tile[tx][ty + 8 * k];
+  }
 }
 
 cudaError_t launch_build_cal(const DevGeom& g, const int2* rowmap, const float* proj_ref, const float* norm,
                              float* cal, cudaStream_t st) {
-  const size_t n = (size_t)g.nang * g.nrad * g.PS;
-  build_cal_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, rowmap, proj_ref, norm, cal, n);
+  const dim3 grid((g.nrad + 31) / 32, (g.PS + 31) / 32, g.nang);
+  build_cal_kernel<<<grid, dim3(32, 8), 0, st>>>(g, rowmap, proj_ref, norm, cal);
   return cudaGetLastError();
 }
 

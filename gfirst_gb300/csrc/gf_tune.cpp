@@ -86,9 +86,9 @@ extern "C" gf_status gf_tune(gf_ctx* c, int32_t* fp_run, int32_t* fp_chunk, int3
       a.padl = f.padl;
       a.cw = f.cw;
       a.lc = f.lc;
-      a.dbg = dbg;
-      a.cal = cal;
-      a.corrcal = c->s_cc;
+      a.fr[0].dbg = dbg;
+      a.fr[0].cal = cal;
+      a.fr[0].corrcal = c->s_cc;
       float ms = 0.f;
       s = time_it([&] { return launch_fp(a, f, st); }, &ms);
       if (s != GF_OK) return done(s);

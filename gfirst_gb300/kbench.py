@@ -1,7 +1,7 @@
 """Kernel micro-benchmark: time one projector stage on a named geometry.
 
     python -m gfirst_gb300.kbench --op bp|fp|subiter [--geometry preclinical] [--subsets 16] [--reps 5]
-                                  [--storage f32|f16|bf16] [--tune]
+                                  [--storage f32|f16|bf16] [--tune] [--bp-form voxel|view]
 
 Runs a mode-1 reconstruction's stages on synthetic data and reports the
 device time per launch from the library's own stage events.  Small enough to
@@ -19,9 +19,11 @@ import gfirst_gb300 as gf
 GEOMS = {"preclinical": gf.Geometry.preclinical, "reference": gf.Geometry.reference, "small": gf.Geometry.small}
 
 
-def run(op: str, geometry: str, nsub: int, reps: int, storage: str = "f32", tune: bool = False) -> dict:
+def run(op: str, geometry: str, nsub: int, reps: int, storage: str = "f32", tune: bool = False,
+        bp_form: str = "voxel") -> dict:
     g = GEOMS[geometry]()
     ctx = gf.Context(g, nsub=nsub)
+    ctx.set_bp_form(bp_form)
     tuned = ctx.tune() if tune else None
     P, ndata, nvox = gf.sizes(g)
     rs = np.random.RandomState(5)
@@ -33,7 +35,8 @@ def run(op: str, geometry: str, nsub: int, reps: int, storage: str = "f32", tune
     r.profile(True)
     for _ in range(reps):
         r.subiteration()
-    out = {"geometry": geometry, "subsets": nsub, "reps": reps, "storage": storage, "tuned": tuned}
+    out = {"geometry": geometry, "subsets": nsub, "reps": reps, "storage": storage, "tuned": tuned,
+           "bp_form": bp_form}
     for name, sid in gf.STAGES.items():
         tot, n = r.profile_read(sid)
         if n:
@@ -51,8 +54,9 @@ def main() -> None:
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--tune", action="store_true")
+    ap.add_argument("--bp-form", default="voxel", choices=["voxel", "view"])
     a = ap.parse_args()
-    print(json.dumps(run(a.op, a.geometry, a.subsets, a.reps, a.storage, a.tune)))
+    print(json.dumps(run(a.op, a.geometry, a.subsets, a.reps, a.storage, a.tune, a.bp_form)))
 
 
 if __name__ == "__main__":

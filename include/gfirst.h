@@ -74,6 +74,7 @@ gf_status gf_lor_index(const gf_geometry* g, int32_t seg_ind, int32_t iz0, int32
  * t with t % nsubsets == s form subset s; nsubsets = 1 is the reference's
  * loop over all angles (NSUBSETS = 1, GFIRST.h:22). */
 gf_status gf_create(const gf_geometry* g, int32_t nsubsets, int32_t device, gf_ctx** out);
+/* Also destroys the reconstructions still open on the context. */
 void gf_destroy(gf_ctx* ctx);
 /* Queue later work on this cudaStream_t (NULL: the context's own stream).  The
  * stream must stay valid while the context queues work on it. */
@@ -89,7 +90,11 @@ gf_status gf_synchronize(gf_ctx* ctx);
  * place of iz + yrot*fz (about 1e-5 relative in the sums) -- and lets voxels
  * outside the segment's planes fall to the gap rule through sentinel rows
  * instead of a range test.  The reference's own hardware interpolation
- * quantises these weights to 1/256. */
+ * quantises these weights to 1/256.  Default GF_BP_PER_VIEW.  The form
+ * applies to gf_back_project and to the doubles image of reconstructions;
+ * triples images (modes 2-3) always take GF_BP_PER_VOXEL: their data are
+ * mostly zero, and where a ratio of 0 meets a gap sentinel the reference's
+ * gap rule turns on whether a weight rounds to exactly 0. */
 enum { GF_BP_PER_VOXEL = 0, GF_BP_PER_VIEW = 1 };
 gf_status gf_set_bp_form(gf_ctx* ctx, int32_t form);
 /* The per-view form's staged-row buffer for a geometry (no device work): a
@@ -206,11 +211,12 @@ typedef struct gf_recon_params {
   int32_t storage; /* per-subset (ratio, mask) sinogram storage: GF_STORE_F32
                       (the reference's precision), GF_STORE_F16 or
                       GF_STORE_BF16; arithmetic stays FP32 */
-  int32_t image_storage; /* storage of the doubles image between
-                            sub-iterations, mode 1 only: GF_STORE_F32 (the
-                            reference), GF_STORE_F16 or GF_STORE_BF16 (every
-                            update rounds the image to 16 bits; arithmetic
-                            stays FP32) */
+  int32_t image_storage; /* storage of the reconstructed images (doubles,
+                            and triples in modes 2-3) between
+                            sub-iterations: GF_STORE_F32 (the reference),
+                            GF_STORE_F16 or GF_STORE_BF16 (every update and
+                            the joint filter's blend round the image to 16
+                            bits; arithmetic stays FP32); not for mode 0 */
 } gf_recon_params;
 
 enum { GF_STORE_F32 = 0, GF_STORE_F16 = 1, GF_STORE_BF16 = 2 };
@@ -266,6 +272,16 @@ void gf_batch_destroy(gf_batch* b);
  * the kernels are launched directly, frame by frame.  Asynchronous. */
 gf_status gf_batch_iterate(gf_batch* b, int32_t n, int32_t use_graph);
 gf_status gf_batch_synchronize(gf_batch* b);
+/* With fused != 0, mode-1 frames that share geometry, subset count, storage,
+ * filters, back-projector form and tile shapes advance as fused groups of up
+ * to 16: every stage of a sub-iteration (forward PSF, projection + ratio,
+ * back projection, update) is one kernel launch over the group's frames,
+ * each frame keeping its own data and results (the same as alone).  Other
+ * frames run on their own as before.  Takes effect at the next iterate. */
+gf_status gf_batch_set_fused(gf_batch* b, int32_t fused);
+/* Units the batch runs (fused groups and single frames) and the size of the
+ * largest group, as they stand now. */
+gf_status gf_batch_groups(gf_batch* b, int32_t* units, int32_t* largest);
 
 /* ---- serving (no counterpart in the reference) ---------------------------- */
 /* Device bytes a reconstruction of these parameters holds (admission control). */

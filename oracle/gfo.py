@@ -76,6 +76,15 @@ class Oracle:
     def a(self, x):
         return np.ascontiguousarray(x, dtype=self.dt)
 
+    def _out(self, buf, n):
+        """A caller's output buffer, written in place by the C oracle: it must
+        hold n elements of this build's real type, contiguous."""
+        if buf is None:
+            return np.zeros(n, self.dt)
+        if buf.dtype != self.dt or buf.size != n or not buf.flags.c_contiguous:
+            raise ValueError(f"output buffer must be {n} contiguous {np.dtype(self.dt).name}")
+        return buf
+
     def segments(self):
         n = self.g.nseg
         idz, zmin, acc = (np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n + 1, np.int32))
@@ -84,12 +93,12 @@ class Oracle:
 
     def fp(self, img, nsub=1, subset=0, out=None):
         img = self.a(img)
-        out = np.zeros(self.ndata, self.dt) if out is None else out
+        out = self._out(out, self.ndata)
         self.L.gfo_fp(ctypes.byref(self.g), _p(img), nsub, subset, _p(out))
         return out
 
     def ratio(self, proj, data, bg, nsub=1, subset=0, corr=None):
-        corr = np.zeros(self.ndata, self.dt) if corr is None else corr
+        corr = self._out(corr, self.ndata)
         self.L.gfo_ratio(ctypes.byref(self.g), _p(self.a(proj)), _p(self.a(data)), _p(self.a(bg)), nsub, subset,
                          _p(corr))
         return corr
