@@ -371,6 +371,22 @@ def run_gpu(args) -> int:
         for k in range(2):  # warm-up: device staging, the geometry projection
             issue(k, wait=True)
             read(k)
+        # where a sequential step's time goes (host clock): the synchronous load,
+        # queueing the iterations, then waiting for them and reading the image
+        phases = {"load_ms": [], "queue_ms": [], "wait_read_ms": []}
+        for k in range(3):
+            t0 = time.perf_counter()
+            gf._ck(lib.gf_recon_load(recs[0].h, None, ptr(host[0][0]), None, ptr(host[0][1]), None,
+                                     gf.ctypes.c_int64(0)))
+            t1 = time.perf_counter()
+            recs[0].iterate(NITER)
+            t2 = time.perf_counter()
+            read(0)
+            t3 = time.perf_counter()
+            phases["load_ms"].append(1000 * (t1 - t0))
+            phases["queue_ms"].append(1000 * (t2 - t1))
+            phases["wait_read_ms"].append(1000 * (t3 - t2))
+        phases = {k: statistics.median(v) for k, v in phases.items()}
         barrier()
         t0 = time.perf_counter()
         for k in range(args.e2e_steps):  # one reconstruction at a time
@@ -392,6 +408,7 @@ def run_gpu(args) -> int:
                "path": "per step: gf_recon_load_async(pinned host sinogram+normalization) + gf_recon_iterate(2) + "
                        "gf_recon_get_image(scaled); two reconstructions on two streams alternate, the next "
                        "step queued before this step's image is read back",
+               "sequential_phases": phases,
                "sequential": {"value": whole_job_rate(world, NSUB * NITER * args.e2e_steps, dt_seq),
                               "ms_per_step": 1000.0 * dt_seq / args.e2e_steps,
                               "path": "gf_recon_load + gf_recon_iterate(2) + gf_recon_get_image, one "
@@ -521,7 +538,10 @@ def run_frames(args) -> int:
     with the default tile shapes.  Batched: FP16 storage of the ratio sinogram,
     autotuned tile shapes, every frame's iteration replayed from one CUDA graph
     (frames run as parallel branches); batched_f32 the same in FP32 storage.
-    Data resident in HBM in every arm."""
+    Fused (and fused_f32): the same graph with the frames of equal subset count
+    fused into groups that run every stage as one launch (gf_batch_set_fused).
+    Data resident in HBM in every arm.  The first and last frames of every arm
+    are compared with the FP64 oracle (--fp64-oracle 0 skips that)."""
     import torch
 
     import gfirst_gb300 as gf
@@ -549,9 +569,15 @@ def run_frames(args) -> int:
 
     def build(storage: str, tune: bool):
         ctxs, recs, tuned = [], [], []
+        shapes = {}  # tuned once per subset count, then set on the other frames' contexts
         for k in range(nf):
             c = gf.Context(g, nsub=int(nsubs[k]))
-            tuned.append(c.tune() if tune else None)
+            if tune and int(nsubs[k]) not in shapes:
+                shapes[int(nsubs[k])] = c.tune()
+            elif tune:
+                t = shapes[int(nsubs[k])]
+                c.set_tile_shapes(t["fp_run"], t["fp_chunk"], t["bp_warps"])
+            tuned.append(shapes.get(int(nsubs[k])) if tune else None)
             r = gf.Recon(c, 1, niter=niter, storage=storage)
             r.load(dsino=data[k][0], norm=data[k][1])
             r._keep = None
@@ -561,10 +587,15 @@ def run_frames(args) -> int:
 
     subiters = int(sum(int(s) * niter for s in nsubs))
     out = {}
-    arms = {"plain": ("f32", False), "batched_f32": ("f32", True), "batched": ("f16", True)}
-    for arm, (storage, batched) in arms.items():
+    check = sorted({0, nf - 1})  # frames whose images are compared with the FP64 oracle
+    imgs = {}
+    arms = {"plain": ("f32", False, False), "batched_f32": ("f32", True, False), "batched": ("f16", True, False),
+            "fused_f32": ("f32", True, True), "fused": ("f16", True, True)}
+    for arm, (storage, batched, fused) in arms.items():
         ctxs, recs, tuned = build(storage, batched)
         batch = gf.Batch(recs) if batched else None
+        if fused:
+            batch.set_fused(True)
 
         def once():
             for r in recs:
@@ -591,8 +622,11 @@ def run_frames(args) -> int:
         clocks = clocks_stop(clk)
         launches = (sum(c.launches() for c in ctxs) - l0) // args.steps
         img0 = recs[0].image()
+        for k in check:
+            imgs[(arm, k)] = recs[k].image()
         out[arm] = {"ms_per_step": 1000.0 * dt, "subiters_per_s": subiters / dt, "frames_per_s": nf / dt,
-                    "storage": storage, "graph": batched,
+                    "storage": storage, "graph": batched, "fused": fused,
+                    "units": batch.groups() if batch is not None else (nf, 1),
                     "gpu_launches_per_step": launches, "clocks": clocks,
                     "tuned": sorted({json.dumps(x, sort_keys=True) for x in tuned if x}) or None,
                     "frame0_image_sum": float(img0.astype(np.float64).sum())}
@@ -603,8 +637,28 @@ def run_frames(args) -> int:
         for c in ctxs:
             c.close()
     rel = abs(out["batched"]["frame0_image_sum"] / out["plain"]["frame0_image_sum"] - 1.0)
-    line = {"metric": METRIC, "value": out["batched"]["subiters_per_s"], "unit": UNIT, "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["batched"]["ms_per_step"],
+
+    def rl2(a, b):
+        return float(np.linalg.norm(np.float64(a) - b) / np.linalg.norm(np.float64(b)))
+
+    # accuracy: the first and last frames of every arm against the FP64 oracle
+    # on the same inputs (test infrastructure, used only as the checker)
+    accuracy = None
+    if args.fp64_oracle:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import gfo
+
+        gfo.build()
+        accuracy = {"tolerance": 1e-3}
+        for k in check:
+            t0 = time.perf_counter()
+            ref = gfo.Oracle(geo, "f64").recon(1, nsub=int(nsubs[k]), niter=niter, dsino=data[k][0],
+                                              norm=data[k][1])["img_d"]
+            accuracy[f"frame{k}"] = {"subsets": int(nsubs[k]), "counts": float(counts[k]),
+                                     "oracle_seconds": time.perf_counter() - t0,
+                                     **{f"{arm}_rel_l2_vs_fp64": rl2(imgs[(arm, k)], ref) for arm in arms}}
+    line = {"metric": METRIC, "value": out["fused"]["subiters_per_s"], "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["fused"]["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 arithmetic",
             "data": "synthetic: seeded body + 10 organs, two-compartment curves, gains U(0.85,1.15), Poisson",
             "config": {"workload": f"{nf} dynamic frames, " + ("preclinical geometry (128x128x159, 128x160x4319)"
@@ -613,9 +667,11 @@ def run_frames(args) -> int:
                        "subsets": [int(x) for x in nsubs], "counts": [float(x) for x in counts],
                        "subiterations_per_step": subiters,
                        "step": "every frame restarted from the cylinder and reconstructed, data resident"},
-            "arms": out, "speedup_batched_vs_plain": out["batched"]["subiters_per_s"] / out["plain"]["subiters_per_s"],
+            "arms": out, "speedup_fused_vs_plain": out["fused"]["subiters_per_s"] / out["plain"]["subiters_per_s"],
+            "speedup_fused_f32_vs_plain": out["fused_f32"]["subiters_per_s"] / out["plain"]["subiters_per_s"],
+            "speedup_batched_vs_plain": out["batched"]["subiters_per_s"] / out["plain"]["subiters_per_s"],
             "speedup_batched_f32_vs_plain": out["batched_f32"]["subiters_per_s"] / out["plain"]["subiters_per_s"],
-            "frame0_sum_rel_diff_f16_vs_f32": rel}
+            "frame0_sum_rel_diff_f16_vs_f32": rel, "accuracy": accuracy}
     print(json.dumps(line))
     return 0
 
@@ -947,10 +1003,12 @@ def run_serving(args) -> int:
         gains = gpu_gains(lam.numel(), 32)
         lv = np.exp(rs.uniform(np.log(1e5), np.log(5e7), 6))
         sinos = [noisy_sinogram(lam, gains, float(x), 40 + i) for i, x in enumerate(lv)]
+        if args.serve_pinned:  # clients hand the server page-locked buffers
+            sinos = [(gf.host_copy(a), gf.host_copy(b)) for a, b in sinos]
         imgs = []
         for i in range(4):
             b, o = ellipsoid_phantom(geo[0], geo[1], 50 + i)
-            imgs.append(b + o)
+            imgs.append(gf.host_copy(b + o) if args.serve_pinned else b + o)
         pool[name] = (g, nsub, sinos, imgs, [float(x) for x in lv])
         del lam, gains
     torch.cuda.empty_cache()
@@ -1104,6 +1162,8 @@ def main() -> int:
     ap.add_argument("--serve-closed", type=int, default=0,
                     help="serving: keep this many requests in flight (closed loop, capacity) instead of the stream")
     ap.add_argument("--serve-requests", type=int, default=300, help="serving, closed loop: requests in all")
+    ap.add_argument("--serve-pinned", type=int, default=1,
+                    help="serving: request inputs in page-locked host memory (0: pageable numpy arrays)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -230,6 +230,9 @@ class Context:
         """Back projector's axial interpolation: "voxel" (GF_BP_PER_VOXEL) or "view" (GF_BP_PER_VIEW)."""
         _ck(lib().gf_set_bp_form(self.h, {"voxel": 0, "view": 1}[form]))
 
+    def set_tile_shapes(self, fp_run: int, fp_chunk: int, bp_warps: int) -> None:
+        _ck(lib().gf_set_tile_shapes(self.h, fp_run, fp_chunk, bp_warps))
+
     def tune(self) -> dict:
         r, lc, w = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
         _ck(lib().gf_tune(self.h, ctypes.byref(r), ctypes.byref(lc), ctypes.byref(w)))
@@ -454,6 +457,40 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+class _Pinned:
+    """Page-locked host memory from gf_host_alloc, freed when the last array over it goes."""
+
+    def __init__(self, nbytes: int):
+        self.p = ctypes.c_void_p()
+        _ck(lib().gf_host_alloc(ctypes.c_size_t(max(int(nbytes), 1)), ctypes.byref(self.p)))
+        self.__array_interface__ = {"shape": (int(nbytes),), "typestr": "|u1", "data": (self.p.value, False),
+                                    "version": 3}
+
+    def __del__(self):
+        try:
+            if self.p:
+                lib().gf_host_free(self.p)
+                self.p = ctypes.c_void_p()
+        except Exception:
+            pass
+
+
+def host_empty(n: int, dtype=np.float32) -> np.ndarray:
+    """An uninitialised numpy array of n elements in page-locked host memory
+    (gf_host_alloc): host<->device copies from it run at the link's speed
+    and overlap with kernels."""
+    dt = np.dtype(dtype)
+    return np.asarray(_Pinned(n * dt.itemsize)).view(dt)
+
+
+def host_copy(a: np.ndarray, dtype=np.float32) -> np.ndarray:
+    """A page-locked copy of array a (flattened)."""
+    a = np.asarray(a, dtype=dtype).ravel()
+    out = host_empty(a.size, dtype)
+    out[:] = a
+    return out
 
 
 def recon_bytes(g: Geometry, nsub: int, mode: int = 1, storage: str = "f32") -> int:

@@ -35,6 +35,22 @@ gf_status upload_runs(gf_ctx* c, const FpSchedule& f) {
 
 }  // namespace
 
+extern "C" gf_status gf_set_tile_shapes(gf_ctx* c, int32_t fp_run, int32_t fp_chunk, int32_t bp_warps) {
+  if (!c) return set_error(GF_ERR_ARG, "null context");
+  if (bp_warps != 4 && bp_warps != 8) return set_error(GF_ERR_ARG, "back-projector warps per block must be 4 or 8");
+  if (fp_run != 9 && fp_run != 17 && fp_run != 25 && fp_run != 33)
+    return set_error(GF_ERR_ARG, "forward-projector run length must be 9, 17, 25 or 33");
+  FpSchedule f;
+  if (!make_fp_schedule(c->plan, fp_run, fp_chunk, &f))
+    return set_error(GF_ERR_GEOMETRY, "no forward-projector schedule with these shapes fits this geometry");
+  GF_CK(cudaSetDevice(c->device));
+  GF_TRY(upload_runs(c, f));
+  c->fps = std::move(f);
+  c->bp_warps = bp_warps;
+  c->gen++;  // graphs captured with the old shapes are stale
+  return GF_OK;
+}
+
 extern "C" gf_status gf_tune(gf_ctx* c, int32_t* fp_run, int32_t* fp_chunk, int32_t* bp_warps) {
   if (!c) return set_error(GF_ERR_ARG, "null context");
   GF_CK(cudaSetDevice(c->device));

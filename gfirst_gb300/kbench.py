@@ -1,7 +1,7 @@
 """Kernel micro-benchmark: time one projector stage on a named geometry.
 
     python -m gfirst_gb300.kbench --op bp|fp|subiter [--geometry preclinical] [--subsets 16] [--reps 5]
-                                  [--storage f32|f16|bf16] [--tune] [--bp-form voxel|view]
+                                  [--storage f32|f16|bf16] [--tune] [--bp-form view|voxel]
 
 Runs a mode-1 reconstruction's stages on synthetic data and reports the
 device time per launch from the library's own stage events.  Small enough to
@@ -20,7 +20,7 @@ GEOMS = {"preclinical": gf.Geometry.preclinical, "reference": gf.Geometry.refere
 
 
 def run(op: str, geometry: str, nsub: int, reps: int, storage: str = "f32", tune: bool = False,
-        bp_form: str = "voxel") -> dict:
+        bp_form: str = "view") -> dict:
     g = GEOMS[geometry]()
     ctx = gf.Context(g, nsub=nsub)
     ctx.set_bp_form(bp_form)
@@ -54,7 +54,7 @@ def main() -> None:
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--tune", action="store_true")
-    ap.add_argument("--bp-form", default="voxel", choices=["voxel", "view"])
+    ap.add_argument("--bp-form", default="view", choices=["voxel", "view"])
     a = ap.parse_args()
     print(json.dumps(run(a.op, a.geometry, a.subsets, a.reps, a.storage, a.tune, a.bp_form)))
 

@@ -339,6 +339,11 @@ gf_status gf_server_get_stats(gf_server* s, gf_server_stats* out);
  * block on this context's geometry with synthetic data, keeps the fastest,
  * and reports them.  Subsequent launches of the context use them. */
 gf_status gf_tune(gf_ctx* ctx, int32_t* fp_run, int32_t* fp_chunk, int32_t* bp_warps);
+/* Sets the tile shapes gf_tune picks (fp_run 9, 17, 25 or 33; fp_chunk 1..256
+ * ray steps per shared-memory chunk; bp_warps 4 or 8), e.g. one context's
+ * tuned shapes on others of the same geometry; GF_ERR_GEOMETRY when the
+ * schedule does not fit the geometry. */
+gf_status gf_set_tile_shapes(gf_ctx* ctx, int32_t fp_run, int32_t fp_chunk, int32_t bp_warps);
 
 /* ---- measurement (no counterpart in the reference, which only prints a
  * one-second wall clock, GFIRST.cu:51-52, 572-573) ------------------------- */
