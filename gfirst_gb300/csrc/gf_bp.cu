@@ -108,34 +108,33 @@ __device__ __forceinline__ void voxel_window(float2 (&acc)[Q], const float (&fiz
 // The voxels of one view, per-view form: the axial fraction and the row
 // offset of the view are shared by every voxel of the column (z = iz + t +
 // 0.5 is taken without the per-voxel rounding, which moves a weight by at
-// most one unit in the last place of iz + t), so the staging has already
-// interpolated along z (S[r] = lerp(R[r], R[r + 1], be)) and lane chunk q
-// reads one staged value rv[32q] at a fixed offset from one per-view
-// pointer.  Voxels outside the segment's plane range read sentinel rows (or
-// a value with weight >= 1/2 on a sentinel pad row): their interpolated mask
-// is negative and the gap rule skips them, as the reference's range test
-// does.
+// most one unit in the last place of iz + t), so lane chunk q reads staged
+// rows rv[32q] and rv[32q + 1] at fixed offsets from one per-view pointer.
+// Voxels outside the segment's plane range read sentinel rows (or a
+// sentinel pad row with weight >= 1/2): their interpolated mask is negative
+// and the gap rule skips them, as the reference's range test does.
 template <int Q, int LO, int HI>
-__device__ __forceinline__ void voxel_views_fast(float2 (&acc)[Q], const float2* rv) {
+__device__ __forceinline__ void voxel_views_fast(float2 (&acc)[Q], const float2* rv, float2 be2) {
 #pragma unroll
   for (int q = LO; q <= HI; q++) {
-    const float2 v = rv[32 * q];
+    const float2 v = lerp2(rv[32 * q], rv[32 * q + 1], be2);
     if (!(v.y < 0.f || v.x < 0.f)) acc[q] = __fadd2_rn(acc[q], v);
   }
 }
 
 // voxel_window for the per-view form (same lane-chunk window).
 template <int Q, int NCH>
-__device__ __forceinline__ void voxel_window_fast(float2 (&acc)[Q], const float2* rv, float t, float zlo) {
+__device__ __forceinline__ void voxel_window_fast(float2 (&acc)[Q], const float2* rv, float2 be2, float t,
+                                                  float zlo) {
   constexpr int W = NCH + 1;  // bp_fast_pads (gf_plan.cpp) sizes the sentinel rows for this window
   if constexpr (W >= Q) {
-    voxel_views_fast<Q, 0, Q - 1>(acc, rv);
+    voxel_views_fast<Q, 0, Q - 1>(acc, rv, be2);
   } else {
     const int izlo = max(__float2int_rd(__fsub_rn(__fsub_rn(zlo, t), 1.0f)), 0);
     switch (min(izlo >> 5, Q - W)) {
 #define GF_VWF(L) \
   case L:         \
-    if constexpr (L <= Q - W) voxel_views_fast<Q, L, L + W - 1>(acc, rv); \
+    if constexpr (L <= Q - W) voxel_views_fast<Q, L, L + W - 1>(acc, rv, be2); \
     break;
       GF_VWF(0) GF_VWF(1) GF_VWF(2) GF_VWF(3) GF_VWF(4) GF_VWF(5) GF_VWF(6)
 #undef GF_VWF
@@ -146,7 +145,7 @@ __device__ __forceinline__ void voxel_window_fast(float2 (&acc)[Q], const float2
 // Row chunks of FP32 pairs loaded during the previous view (the rest load
 // while staging), per back-projector form.
 #ifndef GF_BP_VIEW_PF32
-#define GF_BP_VIEW_PF32 3
+#define GF_BP_VIEW_PF32 4
 #endif
 template <bool FAST>
 constexpr int bp_pf32 = FAST ? GF_BP_VIEW_PF32 : 3;
@@ -190,39 +189,12 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
       __syncwarp();  // every lane is done reading the previous view's rows
       const Pair* q0 = cc + e.x + sg.blk;
       const Pair* q1 = cc + e.y + sg.blk;
-      // the radially interpolated row of lane chunk k (past the segment's rows: the sentinel)
-      auto radial = [&](int k) -> float2 {
+#pragma unroll
+      for (int k = 0; k < NCH; k++) {
         const int r = lane + 32 * k;
-        if (!(k < NCH - 1 || r < nrow)) return make_float2(-1000.f, -1000.f);
-        if (k < PF) return lerp2(pair_f(c0[k < PF ? k : 0]), pair_f(c1[k < PF ? k : 0]), al2);
-        return lerp2(pair_f(__ldg(q0 + r)), pair_f(__ldg(q1 + r)), al2);
-      };
-      // z = iz + t + 0.5 lies between rows floor(t) + iz - zm1 and the next
-      const float ft = floorf(t);
-      const float be = __fsub_rn(t, ft);
-      if constexpr (FAST) {
-        // Per-view form: the axial interpolation with the view's fraction is
-        // done here, once per row, so a voxel reads one staged value:
-        // S[r] = lerp(R[r], R[r + 1], be), R[r + 1] from the next lane (lane
-        // 31: lane 0 of the next chunk), R past the segment's rows = sentinel.
-        const float2 be2 = make_float2(be, be);
-        float2 Rk = radial(0);
-#pragma unroll
-        for (int k = 0; k < NCH; k++) {
-          const float2 Rn = (k + 1 < NCH) ? radial(k + 1) : make_float2(-1000.f, -1000.f);
-          const float2 X = (lane == 0) ? Rn : Rk;
-          float2 up;
-          up.x = __shfl_sync(0xffffffffu, X.x, (lane + 1) & 31);
-          up.y = __shfl_sync(0xffffffffu, X.y, (lane + 1) & 31);
-          const int r = lane + 32 * k;
-          if (k < NCH - 1 || r < nrow) rows[r] = lerp2(Rk, up, be2);
-          Rk = Rn;
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < NCH; k++) {
-          const int r = lane + 32 * k;
-          if (k < NCH - 1 || r < nrow) rows[r] = radial(k);
+        if (k < NCH - 1 || r < nrow) {
+          if (k < PF) rows[r] = lerp2(pair_f(c0[k < PF ? k : 0]), pair_f(c1[k < PF ? k : 0]), al2);
+          else rows[r] = lerp2(pair_f(__ldg(q0 + r)), pair_f(__ldg(q1 + r)), al2);
         }
       }
       __syncwarp();
@@ -231,7 +203,11 @@ __device__ __forceinline__ void segment_views(float2 (&acc)[Q], const float (&fi
         load(e);
       }
       if constexpr (FAST) {
-        voxel_window_fast<Q, NCH>(acc, rows + ((int)ft - zm1) + lane, t, zlo);
+        // z = iz + t + 0.5 lies between rows floor(t) + iz - zm1 and the next
+        const float ft = floorf(t);
+        const float be = __fsub_rn(t, ft);
+        const float2* rv = rows + ((int)ft - zm1) + lane;
+        voxel_window_fast<Q, NCH>(acc, rv, make_float2(be, be), t, zlo);
       } else {
         voxel_window<Q, NCH>(acc, fiz, rows, t, zlo, zhi, zm1, nzs, lane);
       }
