@@ -12,6 +12,8 @@ normalization gains U(0.85, 1.15), Poisson at 5e7 counts.
   python bench.py [--gpus N --steps K --warmup W]    this library on N GPUs (replicas)
   python bench.py --impl reference ...               the CPU restatement of the
                                                      reference path (oracle), all cores
+  python bench.py --impl reference-shim              the reference program's own GPU design
+                                                     (extracted, shimmed textures) on this GPU
   python bench.py --workload frames                  32 dynamic frames: one after another
                                                      in FP32 vs one CUDA graph, FP16 storage
   python bench.py --workload small                   the small configuration in full: GPU vs the
@@ -204,6 +206,103 @@ def run_reference(args) -> int:
                        "parallelism": "host cores (OpenMP)"},
             "cpu_baseline": cpu, "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                                          "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------- reference design on the GPU
+def run_reference_shim(args) -> int:
+    """The reference program's own GPU design on this GPU: its kernels, host
+    wrappers, texture set-up and osem3d()/main(), extracted from the
+    reference sources by oracle/build_ref.py (test infrastructure, in the
+    git-ignored oracle/_ref/) and built with CUDA 13 for sm_103a through
+    oracle/ref_gpu_shim.cuh, which maps the removed texture-reference API on
+    texture objects.  Mode 1 (`gfirst sino.raw norm.raw`) on the preclinical
+    configuration's data, no subsets (the reference's NSUBSETS = 1): one
+    launch of the forward and of the back projector per (segment, angle)
+    view with the host scatter/gather between them.  Wall clock of the whole
+    program at NITER = 2 and NITER = 20; the difference over 18 gives the
+    seconds per iteration.  Beside it, this library on the same data with
+    one subset (the same work per iteration) and its image after 20
+    iterations against the reference program's."""
+    import subprocess
+    import tempfile
+
+    import torch
+
+    import gfirst_gb300 as gf
+
+    if int(os.environ.get("RANK", "0")) != 0:
+        return 0
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import build_ref
+
+    base = {"impl": "reference-shim", "label": "reference design, shimmed"}
+    if not build_ref.gpu_sources_present():
+        print(json.dumps(dict(base, unavailable="the reference's sources were not extracted into oracle/_ref/ "
+                                               "(build_ref.py runs where the reference tree is)")))
+        return 0
+    exes = {n: build_ref.gpu_build("preclinical", n) for n in (2, 20)}
+    torch.cuda.set_device(0)
+    g = gf.Geometry(*GEOM)
+    ctx = gf.Context(g, nsub=NSUB)
+    dimg = ctx.put(phantom())
+    dproj = ctx.array(ctx.ndata).zero()
+    for s_ in range(NSUB):
+        ctx.forward_project(dimg, s_, dproj)
+    proj = dproj.download()
+    dimg.free()
+    dproj.free()
+    ctx.close()
+    dsino, norm = sinogram_from_projection(proj)
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        dd = Path(d)
+        dsino.astype(np.float32).tofile(dd / "sino.raw")
+        norm.astype(np.float32).tofile(dd / "norm.raw")
+
+        def run(n):
+            t0 = time.perf_counter()
+            r = subprocess.run([str(exes[n]), "sino.raw", "norm.raw"], cwd=d, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"reference GPU program failed: {r.stderr[-500:]}")
+            return time.perf_counter() - t0
+
+        run(2)  # first run: driver and module loading
+        clk = clocks_start(0)
+        t2 = min(run(2) for _ in range(2))
+        t20 = run(20)
+        clocks = clocks_stop(clk)
+        ref_img = np.fromfile(dd / "img_GPU_D_ITER20.raw", np.float32)
+    per_iter = (t20 - t2) / 18.0
+    # this library, same data, one subset (one iteration = every view once)
+    c1 = gf.Context(g, nsub=1)
+    tuned = c1.tune()
+    r = gf.Recon(c1, 1, niter=20)
+    r.load(dsino=dsino, norm=norm)
+    r.iterate(2)
+    c1.sync()
+    t0 = time.perf_counter()
+    gf._ck(gf.lib().gf_recon_restart(r.h))
+    r.iterate(20)
+    c1.sync()
+    lib_per_iter = (time.perf_counter() - t0) / 20.0
+    img = r.image(0, scaled=True)
+    r.close()
+    c1.close()
+    rel = float(np.linalg.norm(np.float64(img) - ref_img) / np.linalg.norm(np.float64(ref_img)))
+    line = dict(base, metric="OSEM iterations/s (no subsets)", value=1.0 / per_iter, unit="iter/s", n_gpus=1,
+                steps=20, warmup=2, ms_per_step=1000.0 * per_iter, higher_is_better=True, scaling="weak",
+                vs_baseline=None, dtype="f32 (-use_fast_math, hardware texture filtering)", data=DATA,
+                config={"workload": "preclinical 3D OSEM, mode 1, 128x128x159 image, 128 radial x 160 angles x "
+                                    "4319 planes (span 3, 53 segments), no subsets",
+                        "step": "one iteration of the reference program (every view once), wall clock "
+                                "difference of NITER = 20 and NITER = 2 runs over 18",
+                        "seconds_niter2": t2, "seconds_niter20": t20},
+                library={"ms_per_iteration": 1000.0 * lib_per_iter, "iterations_per_s": 1.0 / lib_per_iter,
+                         "speedup_vs_reference_design": per_iter / lib_per_iter, "tile_shapes": tuned,
+                         "image_rel_l2_vs_reference_gpu_after_20": rel},
+                clocks=clocks)
     print(json.dumps(line))
     return 0
 
@@ -1146,7 +1245,7 @@ def main() -> int:
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference", "reference-shim"])
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=12)
     ap.add_argument("--fp64-steps", type=int, default=4, help="sub-iterations of the FP64 oracle for the "
@@ -1167,6 +1266,8 @@ def main() -> int:
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.impl == "reference-shim":
+        return run_reference_shim(args)
     if args.workload == "frames":
         return run_frames(args)
     if args.workload == "serving":

@@ -40,6 +40,19 @@ KERNEL_FUNCS = [
     "calcGaussianCoefficients", "convolutionXY_GPU", "jointbilateralfilter3D_K",
 ]
 DRIVER_FUNCS = ["osem3d", "main"]
+# The reference's GPU build (ref_gpu_main.cu) also takes its host launch
+# wrappers and texture set-up, and the CPU routines the driver calls.
+GPU_HOST_FUNCS = [
+    "FORWPROJ", "BACKWPROJ", "dividirVxVGPU", "CleanMemory", "UpdateImage", "actualizarCorr", "actualizarCalib",
+    "crearTexturas", "convolutionXY", "jointbilateralfilter3D",
+]
+CPU_FUNCS = ["WriteImage", "CreateInitialCylinder", "ReadImage", "ReadSinogram_Type", "gaussian_filterZ"]
+
+# The preclinical geometry the GPU baseline (ref_gpu_main.cu) is built for.
+GPU_GEOMS = {
+    "preclinical": dict(RES=128, NZS=159, NRAD=128, NANG=160, SPAN=3, NSEG=53, PITCH=1.6, FOV=100.0,
+                        DIAM=165.7758),
+}
 
 # Geometries the golden fixtures use (name -> GFIRST.h constants).
 GEOMS = {
@@ -109,6 +122,8 @@ def main() -> int:
     drv = "".join(extract(REF / "GFIRST.cu", f) for f in DRIVER_FUNCS)
     (OUT / "ref_kernels.inc").write_text(kern)
     (OUT / "ref_driver.inc").write_text(drv)
+    (OUT / "ref_gpu_host.inc").write_text("".join(extract(REF / "GFIRST_GPU_Kernels.cu", f) for f in GPU_HOST_FUNCS))
+    (OUT / "ref_cpu.inc").write_text("".join(extract(REF / "GFIRST_CPU_Kernels.cpp", f) for f in CPU_FUNCS))
     jobs = []
     for name, g in GEOMS.items():
         for tex8 in (False, True):
@@ -128,6 +143,35 @@ def main() -> int:
             print(f"build_ref: {exe.name} failed:\n{err}", file=sys.stderr)
             rc = 1
     return rc
+
+
+def gpu_sources_present() -> bool:
+    return all((OUT / f).exists() for f in ("ref_kernels.inc", "ref_driver.inc", "ref_gpu_host.inc", "ref_cpu.inc"))
+
+
+def gpu_build(name: str = "preclinical", niter: int = 2, force: bool = False) -> Path:
+    """Compiles the reference's GPU program for geometry `name` with NITER =
+    niter, from the sources main() extracted into oracle/_ref/ (they travel
+    with the repository copy; the reference tree itself is not needed
+    here), with the flags of the reference's compile.sh (-O3
+    -use_fast_math) for sm_103a.  Returns the executable's path."""
+    if not gpu_sources_present():
+        raise FileNotFoundError("oracle/_ref/ holds no extracted reference sources (run build_ref.py beside "
+                                "the reference tree)")
+    g = GPU_GEOMS[name]
+    exe = OUT / f"gfirst_refgpu_{name}_n{niter}"
+    if exe.exists() and not force:
+        return exe
+    defs = [f"-DGFR_{k}={v}" for k, v in g.items() if k not in ("PITCH", "FOV", "DIAM")]
+    defs += [f"-DGFR_PITCH={g['PITCH']}f", f"-DGFR_FOV={g['FOV']}f", f"-DGFR_DIAM={g['DIAM']}f",
+             f"-DGFR_NSINOGS={planes(g)}", f"-DGFR_NITER={niter}"]
+    nvcc = os.environ.get("CUDA_HOME", "/usr/local/cuda") + "/bin/nvcc"
+    cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-use_fast_math", "-std=c++17", "-w",
+           "--expt-extended-lambda", f"-I{HERE}", f"-I{OUT}", *defs, str(HERE / "ref_gpu_main.cu"), "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference GPU build failed:\n" + r.stderr[-3000:])
+    return exe
 
 
 if __name__ == "__main__":
