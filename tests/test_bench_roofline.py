@@ -39,4 +39,4 @@ def test_committed_traffic_covers_both_projectors():
         assert e["warp_instructions"] > 0 and 0 < e["issue_active_pct"] <= 100
         # DRAM traffic within 15 % of the compulsory bytes: nothing re-read
         assert abs(e["bytes_per_launch"] / alg[k] - 1) < 0.15
-    assert "ncu" in t["command"] and "--clock-control none" in t["command"]
+        assert "ncu" in e["command"] and "--clock-control none" in e["command"]
