@@ -638,7 +638,9 @@ def run_frames(args) -> int:
     autotuned tile shapes, every frame's iteration replayed from one CUDA graph
     (frames run as parallel branches); batched_f32 the same in FP32 storage.
     Fused (and fused_f32): the same graph with the frames of equal subset count
-    fused into groups that run every stage as one launch (gf_batch_set_fused).
+    fused into groups that run every stage as one launch, the back projection
+    two frames per warp (the frames share the scanner's normalization);
+    fused_launch_only: the groups with one frame per warp (gf_batch_set_fused).
     Data resident in HBM in every arm.  The first and last frames of every arm
     are compared with the FP64 oracle (--fp64-oracle 0 skips that)."""
     import torch
@@ -688,13 +690,14 @@ def run_frames(args) -> int:
     out = {}
     check = sorted({0, nf - 1})  # frames whose images are compared with the FP64 oracle
     imgs = {}
-    arms = {"plain": ("f32", False, False), "batched_f32": ("f32", True, False), "batched": ("f16", True, False),
-            "fused_f32": ("f32", True, True), "fused": ("f16", True, True)}
+    # fused: 0 no, 1 groups with frame pairs back-projected together, 2 groups only
+    arms = {"plain": ("f32", False, 0), "batched_f32": ("f32", True, 0), "batched": ("f16", True, 0),
+            "fused_launch_only": ("f16", True, 2), "fused_f32": ("f32", True, 1), "fused": ("f16", True, 1)}
     for arm, (storage, batched, fused) in arms.items():
         ctxs, recs, tuned = build(storage, batched)
         batch = gf.Batch(recs) if batched else None
         if fused:
-            batch.set_fused(True)
+            batch.set_fused(True, pairs=fused == 1)
 
         def once():
             for r in recs:
@@ -725,7 +728,7 @@ def run_frames(args) -> int:
             imgs[(arm, k)] = recs[k].image()
         out[arm] = {"ms_per_step": 1000.0 * dt, "subiters_per_s": subiters / dt, "frames_per_s": nf / dt,
                     "storage": storage, "graph": batched, "fused": fused,
-                    "units": batch.groups() if batch is not None else (nf, 1),
+                    "units": batch.groups() if batch is not None else (nf, 1, 0),
                     "gpu_launches_per_step": launches, "clocks": clocks,
                     "tuned": sorted({json.dumps(x, sort_keys=True) for x in tuned if x}) or None,
                     "frame0_image_sum": float(img0.astype(np.float64).sum())}

@@ -361,15 +361,17 @@ class Batch:
         _ck(lib().gf_batch_create(len(self.recons), arr, ctypes.byref(h)))
         self.h = h
 
-    def set_fused(self, fused: bool = True) -> None:
-        """Fused groups: frames that match run each stage as one launch (gf_batch_set_fused)."""
-        _ck(lib().gf_batch_set_fused(self.h, int(fused)))
+    def set_fused(self, fused: bool = True, pairs: bool = True) -> None:
+        """Fused groups: frames that match run each stage as one launch; with
+        pairs, frames of equal normalization back-project two per warp
+        (gf_batch_set_fused 1, else 2; fused=False: 0)."""
+        _ck(lib().gf_batch_set_fused(self.h, 0 if not fused else (1 if pairs else 2)))
 
     def groups(self) -> tuple:
-        """(units, largest group) as the batch stands now."""
-        n, big = ctypes.c_int32(), ctypes.c_int32()
-        _ck(lib().gf_batch_groups(self.h, ctypes.byref(n), ctypes.byref(big)))
-        return n.value, big.value
+        """(units, largest group, frame pairs back-projected together) as the batch stands now."""
+        n, big, pr = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _ck(lib().gf_batch_groups(self.h, ctypes.byref(n), ctypes.byref(big), ctypes.byref(pr)))
+        return n.value, big.value, pr.value
 
     def iterate(self, n: int = 1, graph: bool = True) -> None:
         _ck(lib().gf_batch_iterate(self.h, n, int(graph)))

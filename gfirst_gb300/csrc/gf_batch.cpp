@@ -5,7 +5,10 @@
 // (gf_batch_set_fused), mode-1 frames that share geometry, subset count,
 // storage, filters and tile shapes form fused groups of up to kMaxFrames,
 // whose sub-iterations run every stage as one launch over the group
-// (fused_subiteration); every other frame is a unit of its own.
+// (fused_subiteration); every other frame is a unit of its own.  In a group
+// whose frames' normalization masks are equal (the frames of one scanner
+// and normalization), the back projection runs two frames per warp, sharing
+// the per-view geometry and the mask rows.
 //
 // One iteration of every unit is captured once: a fork event on the batch's
 // origin stream, each unit's kernels on the stream of its first frame (a
@@ -29,8 +32,10 @@ using namespace gf;
 struct gf_batch {
   std::vector<gf_recon*> frames;
   int device = 0;
-  bool fused = false;
+  int fused = 0;  // gf_batch_set_fused: 0 off, 1 groups (paired back projection where masks match), 2 groups
   std::vector<std::vector<int>> units;  // frame indices: a fused group, or one frame
+  std::vector<bool> shared_mask;        // per unit: every frame's normalization mask equals the first's
+  int* d_flag = nullptr;                // device flag of the mask comparison
   cudaStream_t origin = nullptr;
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> joins;  // one per frame (a unit uses its first frame's)
@@ -73,12 +78,43 @@ static void make_units(gf_batch* b) {
   }
 }
 
+// Which fused groups may back-project two frames per warp: those whose
+// frames' static normalization masks (every subset) are equal to the first
+// frame's, bit for bit, compared on the device after the frames' queued work
+// (their loads) has finished.
+static gf_status check_masks(gf_batch* b) {
+  b->shared_mask.assign(b->units.size(), false);
+  if (b->fused != 1) return GF_OK;
+  for (size_t k = 0; k < b->units.size(); k++) {
+    const auto& u = b->units[k];
+    if (u.size() < 2) continue;
+    const gf_recon* r0 = b->frames[u[0]];
+    if (r0->ctx->bp_form != GF_BP_PER_VIEW) continue;
+    bool same = true;
+    for (size_t j = 1; j < u.size() && same; j++) {
+      const gf_recon* r = b->frames[u[j]];
+      GF_CK(cudaStreamSynchronize(r0->ctx->stream));
+      GF_CK(cudaStreamSynchronize(r->ctx->stream));
+      if (r->cal == r0->cal) continue;
+      GF_CK(launch_differs(r0->cal, r->cal, (size_t)r0->ctx->plan.all_elems(), b->d_flag, b->origin));
+      int flag = 1;
+      GF_CK(cudaMemcpyAsync(&flag, b->d_flag, sizeof(int), cudaMemcpyDeviceToHost, b->origin));
+      GF_CK(cudaStreamSynchronize(b->origin));
+      same = flag == 0;
+    }
+    b->shared_mask[k] = same;
+  }
+  return GF_OK;
+}
+
 // One iteration of one unit on its first frame's stream.
-static gf_status unit_iteration(gf_batch* b, const std::vector<int>& u) {
+static gf_status unit_iteration(gf_batch* b, size_t k) {
+  const std::vector<int>& u = b->units[k];
   if (u.size() == 1) return gf_recon_iterate(b->frames[u[0]], 1);
   std::vector<gf_recon*> G;
   for (int i : u) G.push_back(b->frames[i]);
-  for (int k = 0; k < G[0]->ctx->plan.nsub; k++) GF_TRY(fused_subiteration(G.data(), (int)G.size()));
+  for (int s = 0; s < G[0]->ctx->plan.nsub; s++)
+    GF_TRY(fused_subiteration(G.data(), (int)G.size(), b->shared_mask[k]));
   return GF_OK;
 }
 
@@ -104,6 +140,7 @@ gf_status gf_batch_create(int32_t n, gf_recon* const* frames, gf_batch** out) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   b->joins.assign(n, nullptr);
   for (int i = 0; i < n && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&b->joins[i], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_flag, sizeof(int));
   if (e != cudaSuccess) {
     gf_batch_destroy(b);
     return cuda_error(e, "batch set-up");
@@ -121,29 +158,35 @@ void gf_batch_destroy(gf_batch* b) {
     if (ev) cudaEventDestroy(ev);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->origin) cudaStreamDestroy(b->origin);
+  if (b->d_flag) cudaFree(b->d_flag);
   delete b;
 }
 
 gf_status gf_batch_set_fused(gf_batch* b, int32_t fused) {
   if (!b) return set_error(GF_ERR_ARG, "null batch");
-  if ((fused != 0) == b->fused) return GF_OK;
+  if (fused < 0 || fused > 2) return set_error(GF_ERR_ARG, "fused must be 0, 1 or 2");
+  if (fused == b->fused) return GF_OK;
   GF_CK(cudaSetDevice(b->device));
   GF_CK(cudaStreamSynchronize(b->origin));  // a queued replay may still use the graph
   drop_graph(b);
-  b->fused = fused != 0;
+  b->fused = fused;
   make_units(b);
   return GF_OK;
 }
 
-gf_status gf_batch_groups(gf_batch* b, int32_t* ngroups, int32_t* largest) {
+gf_status gf_batch_groups(gf_batch* b, int32_t* ngroups, int32_t* largest, int32_t* paired) {
   if (!b) return set_error(GF_ERR_ARG, "null batch");
-  int n = 0, big = 0;
-  for (auto& u : b->units) {
+  GF_CK(cudaSetDevice(b->device));
+  GF_TRY(check_masks(b));
+  int n = 0, big = 0, pairs = 0;
+  for (size_t k = 0; k < b->units.size(); k++) {
     n++;
-    big = std::max(big, (int)u.size());
+    big = std::max(big, (int)b->units[k].size());
+    if (b->shared_mask[k]) pairs += (int)b->units[k].size() / 2;
   }
   if (ngroups) *ngroups = n;
   if (largest) *largest = big;
+  if (paired) *paired = pairs;
   return GF_OK;
 }
 
@@ -157,6 +200,7 @@ static gf_status capture(gf_batch* b) {
   make_units(b);
   // the frames' streams must be idle before they join the capture
   for (gf_recon* r : b->frames) GF_CK(cudaStreamSynchronize(r->ctx->stream));
+  GF_TRY(check_masks(b));
   std::vector<bool> prof(b->frames.size());
   std::vector<gf_ctx*> ctxs;  // each context once: frames may share one
   std::vector<int64_t> l0;
@@ -177,7 +221,7 @@ static gf_status capture(gf_batch* b) {
     cudaStream_t s = b->frames[first]->ctx->stream;
     e = cudaStreamWaitEvent(s, b->fork, 0);
     if (e != cudaSuccess) break;
-    st = unit_iteration(b, b->units[k]);
+    st = unit_iteration(b, k);
     if (st == GF_OK) e = cudaEventRecord(b->joins[first], s);
     if (e == cudaSuccess && st == GF_OK) e = cudaStreamWaitEvent(b->origin, b->joins[first], 0);
   }
@@ -227,8 +271,10 @@ gf_status gf_batch_iterate(gf_batch* b, int32_t n, int32_t use_graph) {
   GF_CK(cudaSetDevice(b->device));
   if (!use_graph) {
     make_units(b);
+    GF_TRY(check_masks(b));
     for (int it = 0; it < n; it++) {
-      for (auto& u : b->units) {
+      for (size_t ku = 0; ku < b->units.size(); ku++) {
+        const std::vector<int>& u = b->units[ku];
         // a fused group runs on its first frame's stream: it waits for the
         // other frames' queued work, and their later work waits for it
         cudaStream_t s0 = b->frames[u[0]]->ctx->stream;
@@ -236,7 +282,7 @@ gf_status gf_batch_iterate(gf_batch* b, int32_t n, int32_t use_graph) {
           GF_CK(cudaEventRecord(b->joins[u[k]], b->frames[u[k]]->ctx->stream));
           GF_CK(cudaStreamWaitEvent(s0, b->joins[u[k]], 0));
         }
-        GF_TRY(unit_iteration(b, u));
+        GF_TRY(unit_iteration(b, ku));
         if (u.size() > 1) {
           GF_CK(cudaEventRecord(b->joins[u[0]], s0));
           for (size_t k = 1; k < u.size(); k++)

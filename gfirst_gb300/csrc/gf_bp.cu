@@ -287,6 +287,251 @@ __device__ __forceinline__ void bp_column(const BpArgs& a, int rmax) {
   }
 }
 
+// ---- two frames per warp ------------------------------------------------
+// Two frames of a fused group whose normalization masks are equal share one
+// warp per column: the per-(column, angle) table, the per-view fraction, row
+// offset and lane-chunk window, and the staged mask rows with their
+// interpolation; only the ratios and the (NUMER, DENOM) sums are per frame.
+// A staged row holds (ratio A, ratio B) and the mask, 12 bytes instead of
+// two frames' 16, and each frame's row loads fetch only its ratio beside
+// frame A's (ratio, mask) pair.  Every operation on a frame's values is the
+// per-view form's (the packed f32x2 operations round each element as the
+// scalar one), so each frame's sums equal the per-view form's for that frame
+// alone, bit for bit.
+
+__device__ __forceinline__ float ratio_of(const float2* p) { return *reinterpret_cast<const float*>(p); }
+__device__ __forceinline__ float ratio_of(const __half2* p) { return __half2float(*reinterpret_cast<const __half*>(p)); }
+__device__ __forceinline__ float ratio_of(const __nv_bfloat162* p) {
+  return __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(p));
+}
+
+template <int Q, int LO, int HI>
+__device__ __forceinline__ void voxel_views_pair(float2 (&accA)[Q], float2 (&accB)[Q], const float2* rr,
+                                                 const float* rc, float be) {
+  const float2 be2 = make_float2(be, be);
+#pragma unroll
+  for (int q = LO; q <= HI; q++) {
+    const float2 vr = lerp2(rr[32 * q], rr[32 * q + 1], be2);  // (ratio A, ratio B)
+    const float vc = lerp_rn(rc[32 * q], rc[32 * q + 1], be);    // mask
+    if (!(vc < 0.f || vr.x < 0.f)) accA[q] = __fadd2_rn(accA[q], make_float2(vr.x, vc));
+    if (!(vc < 0.f || vr.y < 0.f)) accB[q] = __fadd2_rn(accB[q], make_float2(vr.y, vc));
+  }
+}
+
+template <int Q, int NCH>
+__device__ __forceinline__ void voxel_window_pair(float2 (&accA)[Q], float2 (&accB)[Q], const float2* rr,
+                                                  const float* rc, float be, float t, float zlo) {
+  constexpr int W = NCH + 1;  // the per-view form's window (bp_fast_pads sizes the sentinel rows for it)
+  if constexpr (W >= Q) {
+    voxel_views_pair<Q, 0, Q - 1>(accA, accB, rr, rc, be);
+  } else {
+    const int izlo = max(__float2int_rd(__fsub_rn(__fsub_rn(zlo, t), 1.0f)), 0);
+    switch (min(izlo >> 5, Q - W)) {
+#define GF_VWP(L) \
+  case L:         \
+    if constexpr (L <= Q - W) voxel_views_pair<Q, L, L + W - 1>(accA, accB, rr, rc, be); \
+    break;
+      GF_VWP(0) GF_VWP(1) GF_VWP(2) GF_VWP(3) GF_VWP(4) GF_VWP(5) GF_VWP(6)
+#undef GF_VWP
+    }
+  }
+}
+
+#ifndef GF_BP_PAIR_PF32
+#define GF_BP_PAIR_PF32 2
+#endif
+#ifndef GF_BP_PAIR_PF16
+#define GF_BP_PAIR_PF16 3
+#endif
+
+template <int Q, int NCH, class Pair>
+__device__ __forceinline__ void segment_views_pair(float2 (&accA)[Q], float2 (&accB)[Q], const Pair* ccA,
+                                                   const Pair* ccB, const int4* my, float2* rr, float* rc,
+                                                   const DevSeg& sg, int na, int lane) {
+  const float zlo = (float)sg.zmin;
+  const int zm1 = sg.zmin - 1;
+  const int nrow = sg.nplanes + 2;
+  // next view's rows loaded during the current view's voxels (the first
+  // GF_BP_PAIR_PF32 / GF_BP_PAIR_PF16 chunks; the rest at staging)
+  constexpr int PFC = sizeof(Pair) == 8 ? GF_BP_PAIR_PF32 : GF_BP_PAIR_PF16;
+  constexpr int PF = NCH > PFC ? PFC : NCH;
+  Pair a0[PF], a1[PF];
+  float b0[PF], b1[PF];
+  auto load = [&](const int4& e) {
+    const Pair* pa0 = ccA + e.x + sg.blk;
+    const Pair* pa1 = ccA + e.y + sg.blk;
+    const Pair* pb0 = ccB + e.x + sg.blk;
+    const Pair* pb1 = ccB + e.y + sg.blk;
+#pragma unroll
+    for (int k = 0; k < PF; k++) {
+      const int r = lane + 32 * k;
+      if (k < NCH - 1 || r < nrow) {
+        a0[k] = __ldg(pa0 + r);
+        a1[k] = __ldg(pa1 + r);
+        b0[k] = ratio_of(pb0 + r);
+        b1[k] = ratio_of(pb1 + r);
+      }
+    }
+  };
+  int4 e = my[0];
+  load(e);
+  for (int tl = 0; tl < na; tl++) {
+    const float al = __int_as_float(e.z);
+    const float2 al2 = make_float2(al, al);
+    const float t = __fmul_rn(__int_as_float(e.w), sg.fz);  // yrot*fz
+    __syncwarp();  // every lane is done reading the previous view's rows
+    const Pair* qa0 = ccA + e.x + sg.blk;
+    const Pair* qa1 = ccA + e.y + sg.blk;
+    const Pair* qb0 = ccB + e.x + sg.blk;
+    const Pair* qb1 = ccB + e.y + sg.blk;
+#pragma unroll
+    for (int k = 0; k < NCH; k++) {
+      const int r = lane + 32 * k;
+      if (k < NCH - 1 || r < nrow) {
+        float2 va;
+        float vb;
+        if (k < PF) {
+          va = lerp2(pair_f(a0[k < PF ? k : 0]), pair_f(a1[k < PF ? k : 0]), al2);
+          vb = lerp_rn(b0[k < PF ? k : 0], b1[k < PF ? k : 0], al);
+        } else {
+          va = lerp2(pair_f(__ldg(qa0 + r)), pair_f(__ldg(qa1 + r)), al2);
+          vb = lerp_rn(ratio_of(qb0 + r), ratio_of(qb1 + r), al);
+        }
+        rr[r] = make_float2(va.x, vb);
+        rc[r] = va.y;
+      }
+    }
+    __syncwarp();
+    if (tl + 1 < na) {
+      e = my[tl + 1];
+      load(e);
+    }
+    const float ft = floorf(t);
+    const float be = __fsub_rn(t, ft);
+    const int off = ((int)ft - zm1) + lane;
+    voxel_window_pair<Q, NCH>(accA, accB, rr + off, rc + off, be, t, zlo);
+  }
+}
+
+// a.fr[2p] and a.fr[2p + 1] form pair p = blockIdx.y; staged rows per warp:
+// rmax = rbuf float2 (ratios) + rbuf floats (mask).
+template <int Q, int STORE>
+__device__ __forceinline__ void bp_column_pair(const BpArgs& a, int rmax) {
+  using Pair = typename PairT<STORE>::type;
+  const BpFrame& FA = a.fr[2 * blockIdx.y];
+  const BpFrame& FB = a.fr[2 * blockIdx.y + 1];
+  const Pair* ccA = static_cast<const Pair*>(FA.corrcal);
+  const Pair* ccB = static_cast<const Pair*>(FB.corrcal);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const DevGeom& g = a.g;
+  const int nwarps = blockDim.x >> 5;
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int colidx = blockIdx.x * nwarps + wib;
+  if (colidx >= g.res * g.res) return;  // whole warp
+  const int iy = colidx / g.res, ix = colidx - iy * g.res;
+  int4* my = reinterpret_cast<int4*>(smraw) + wib * a.na;
+  float2* rr = reinterpret_cast<float2*>(reinterpret_cast<int4*>(smraw) + nwarps * a.na) + wib * rmax;
+  float* rc = reinterpret_cast<float*>(reinterpret_cast<float2*>(reinterpret_cast<int4*>(smraw) + nwarps * a.na) +
+                                       nwarps * rmax) + wib * rmax;
+  for (int r = lane; r < rmax; r += 32) {
+    rr[r] = make_float2(-1000.f, -1000.f);
+    rc[r] = -1000.f;
+  }
+  rr += a.pad_lo;
+  rc += a.pad_lo;
+  // per angle: radial texels, weight and yrot (GFIRST_GPU_Kernels.cu:136-147)
+  const float xv = __fsub_rn((float)ix, g.resm), yv = __fsub_rn((float)iy, g.resm);
+  for (int tl = lane; tl < a.na; tl += 32) {
+    const float2 sc = g.trig[subset_angle(g, a.subset, tl)];
+    const float xrot = __fadd_rn(__fmul_rn(xv, sc.y), __fmul_rn(yv, sc.x));
+    const float yrot = __fadd_rn(__fmul_rn(-xv, sc.x), __fmul_rn(yv, sc.y));
+    const float x = __fadd_rn(__fadd_rn(g.radm, __fmul_rn(xrot, g.fx_bp)), 0.5f);
+    const float xb = __fsub_rn(x, 0.5f);
+    const float fl = floorf(xb);
+    const int i = (int)fl;
+    const int i0 = clampi(i, 0, g.nrad - 1), i1 = clampi(i + 1, 0, g.nrad - 1);
+    const int rb = tl * g.nrad;
+    my[tl] = make_int4((rb + i0) * g.PS, (rb + i1) * g.PS, __float_as_int(__fsub_rn(xb, fl)), __float_as_int(yrot));
+  }
+  __syncwarp();
+  float2 accA[Q], accB[Q];
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    accA[q] = make_float2(0.f, 0.f);
+    accB[q] = make_float2(0.f, 0.f);
+  }
+  for (int s = 0; s < g.nseg; s++) {
+    const DevSeg sg = g.seg[s];
+    __syncwarp();
+    const int nrow = sg.nplanes + 2;
+    for (int r = nrow + lane; r < rmax - a.pad_lo; r += 32) {
+      rr[r] = make_float2(-1000.f, -1000.f);
+      rc[r] = -1000.f;
+    }
+    switch ((sg.nplanes + 2 + 31) >> 5) {
+#define GF_SEGP(N) \
+  case N:          \
+    if constexpr (N <= Q + 1) segment_views_pair<Q, N>(accA, accB, ccA, ccB, my, rr, rc, sg, a.na, lane); \
+    break;
+      GF_SEGP(1) GF_SEGP(2) GF_SEGP(3) GF_SEGP(4) GF_SEGP(5) GF_SEGP(6) GF_SEGP(7) GF_SEGP(8) GF_SEGP(9)
+#undef GF_SEGP
+    }
+  }
+  const size_t cb = (size_t)colidx * g.nzp;
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const int iz = lane + 32 * q;
+    FA.numer[cb + iz] = iz < g.nzs ? accA[q].x : 0.f;
+    FA.denom[cb + iz] = iz < g.nzs ? accA[q].y : 0.f;
+    FB.numer[cb + iz] = iz < g.nzs ? accB[q].x : 0.f;
+    FB.denom[cb + iz] = iz < g.nzs ? accB[q].y : 0.f;
+  }
+}
+
+#ifndef GF_BP_PAIR_REGS
+#define GF_BP_PAIR_REGS 80
+#endif
+
+template <int STORE>
+constexpr int bp_pair_regs = GF_BP_PAIR_REGS;
+
+template <int Q, int STORE>
+__global__ void __launch_bounds__(256) __maxnreg__(bp_pair_regs<STORE>) bp_pair_kernel(const BpArgs a, int rmax) {
+  bp_column_pair<Q, STORE>(a, rmax);
+}
+
+cudaError_t launch_bp_pairs(const BpArgs& a, int warps, cudaStream_t st) {
+  if (warps < 1 || warps > 8) return cudaErrorInvalidValue;
+  if (!a.fast || a.pad_lo < 0 || a.rbuf < a.pad_lo + a.g.nzs + 2) return cudaErrorInvalidValue;
+  const int npairs = a.nfr / 2;
+  if (npairs < 1 || 2 * npairs != a.nfr || a.nfr > kMaxFrames) return cudaErrorInvalidValue;
+  for (int f = 0; f < a.nfr; f++)
+    if (!a.fr[f].corrcal || !a.fr[f].numer || !a.fr[f].denom) return cudaErrorInvalidValue;
+  const int Q = a.g.nzp / 32;
+  const int rmax = a.rbuf;
+  dim3 grid((a.g.res * a.g.res + warps - 1) / warps, npairs);
+  size_t smem = (size_t)warps * (a.na * sizeof(int4) + rmax * (sizeof(float2) + sizeof(float)));
+  void (*k)(BpArgs, int) = nullptr;
+  switch (a.storage * 16 + Q) {
+#define GF_BPP_CASE(S, QQ) \
+  case S * 16 + QQ: k = bp_pair_kernel<QQ, S>; break;
+    GF_BPP_CASE(0, 1) GF_BPP_CASE(0, 2) GF_BPP_CASE(0, 3) GF_BPP_CASE(0, 4)
+    GF_BPP_CASE(0, 5) GF_BPP_CASE(0, 6) GF_BPP_CASE(0, 7) GF_BPP_CASE(0, 8)
+    GF_BPP_CASE(1, 1) GF_BPP_CASE(1, 2) GF_BPP_CASE(1, 3) GF_BPP_CASE(1, 4)
+    GF_BPP_CASE(1, 5) GF_BPP_CASE(1, 6) GF_BPP_CASE(1, 7) GF_BPP_CASE(1, 8)
+    GF_BPP_CASE(2, 1) GF_BPP_CASE(2, 2) GF_BPP_CASE(2, 3) GF_BPP_CASE(2, 4)
+    GF_BPP_CASE(2, 5) GF_BPP_CASE(2, 6) GF_BPP_CASE(2, 7) GF_BPP_CASE(2, 8)
+#undef GF_BPP_CASE
+    default: return cudaErrorInvalidValue;
+  }
+  if (smem > 48 * 1024) {
+    cudaError_t e = allow_max_smem(k);
+    if (e != cudaSuccess) return e;
+  }
+  k<<<grid, warps * 32, smem, st>>>(a, rmax);
+  return cudaGetLastError();
+}
+
 // Register budgets.  The kernel hides its latencies with resident warps: up
 // to 160 slices both pair types are capped at 64 registers (eight 4-warp
 // blocks per SM, no spill; FP32 with the shallower prefetch above) -- 1.296

@@ -158,5 +158,7 @@ bool fusable(const gf_recon* a, const gf_recon* b);
 // subset): the forward PSF, projection + ratio, back projection and update
 // are one launch each over the nfr <= kMaxFrames frames, on the first
 // frame's stream and with its tables.  Advances every frame's cursor.
-gf_status fused_subiteration(gf_recon* const* G, int nfr);
+// With shared_mask (every frame's normalization mask equal to the first's,
+// per-view back projector) the back projection runs two frames per warp.
+gf_status fused_subiteration(gf_recon* const* G, int nfr, bool shared_mask = false);
 }  // namespace gf

@@ -61,6 +61,9 @@ struct BpArgs {
   int pad_lo, rbuf;        // fast form: staged-row buffer per warp (BpPads)
 };
 cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st);
+// Per-view form over a.nfr = 2n frames as n pairs (frames 2p, 2p + 1) that
+// share their normalization mask: one warp per column and pair.
+cudaError_t launch_bp_pairs(const BpArgs& a, int warps, cudaStream_t st);
 // Lets kernel k use up to the device's opt-in shared memory per block.  Every
 // call sets the same value, so host threads that launch one kernel with
 // different shared-memory sizes at the same time cannot undo each other's
@@ -127,6 +130,8 @@ cudaError_t launch_ratio_file(const DevGeom& g, int subset, const float* proj, c
                               float* corr, cudaStream_t st);
 cudaError_t launch_norm_mask(const DevGeom& g, const float* proj_blank, const float* blank, float* calib,
                              cudaStream_t st);
+// *flag = 1 (device int) when the n floats of a and b differ anywhere.
+cudaError_t launch_differs(const float* a, const float* b, size_t n, int* flag, cudaStream_t st);
 cudaError_t launch_vlor_count(const DevGeom& g, const int32_t* ev, long long nev, float* cnt, cudaStream_t st);
 cudaError_t launch_blankt(const DevGeom& g, const float* cnt, const float* tsino_raw, float* blankt,
                           cudaStream_t st);

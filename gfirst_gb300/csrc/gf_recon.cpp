@@ -169,7 +169,7 @@ bool fusable(const gf_recon* a, const gf_recon* b) {
          x->bp_form == y->bp_form && x->bp_warps == y->bp_warps && x->fps.R == y->fps.R && x->fps.lc == y->fps.lc;
 }
 
-gf_status fused_subiteration(gf_recon* const* G, int nfr) {
+gf_status fused_subiteration(gf_recon* const* G, int nfr, bool shared_mask) {
   if (nfr < 1 || nfr > kMaxFrames) return set_error(GF_ERR_ARG, "fused group size out of range");
   gf_recon* r0 = G[0];
   gf_ctx* c = r0->ctx;
@@ -193,9 +193,22 @@ gf_status fused_subiteration(gf_recon* const* G, int nfr) {
     a.fr[k] = FpFrame{G[k]->psf, G[k]->dbg[0] + off, G[k]->cal + off, G[k]->corrcal, nullptr};
   GF_LAUNCH(c, launch_fp(a, c->fps, st));
   BpArgs b = c->bp_args(s, r0->corrcal, r0->numer, r0->denom, r0->p.storage);
-  b.nfr = nfr;
-  for (int k = 0; k < nfr; k++) b.fr[k] = BpFrame{G[k]->corrcal, G[k]->numer, G[k]->denom};
-  GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
+  const int npair = (shared_mask && b.fast) ? nfr / 2 : 0;
+  if (npair > 0) {
+    // frames 2p and 2p + 1 share a warp per column; an odd last frame alone
+    b.nfr = 2 * npair;
+    for (int k = 0; k < 2 * npair; k++) b.fr[k] = BpFrame{G[k]->corrcal, G[k]->numer, G[k]->denom};
+    GF_LAUNCH(c, launch_bp_pairs(b, c->bp_warps, st));
+    if (nfr > 2 * npair) {
+      b.nfr = 1;
+      b.fr[0] = BpFrame{G[nfr - 1]->corrcal, G[nfr - 1]->numer, G[nfr - 1]->denom};
+      GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
+    }
+  } else {
+    b.nfr = nfr;
+    for (int k = 0; k < nfr; k++) b.fr[k] = BpFrame{G[k]->corrcal, G[k]->numer, G[k]->denom};
+    GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
+  }
   ImgFrames u{};
   for (int k = 0; k < nfr; k++) u.fr[k] = ImgFrame{G[k]->numer, G[k]->denom, G[k]->ctmp, G[k]->img[0]};
   GF_LAUNCH(c, launch_conv_xy_frames(c->dg, u, nfr, true, r0->g_bw, st));

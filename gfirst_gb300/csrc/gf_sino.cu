@@ -221,6 +221,22 @@ __global__ void norm_mask_kernel(const float* __restrict__ pb, const float* __re
   c[i] = ((double)pb[i] > 0.01 && (double)b[i] > 0.01) ? 1.0f : -1000.f;
 }
 
+// *flag = 1 when a and b differ anywhere in their n floats (bitwise); *flag
+// must hold 0 before.
+__global__ void differs_kernel(const float* __restrict__ a, const float* __restrict__ b, size_t n, int* flag) {
+  int d = 0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    d |= __float_as_int(a[i]) ^ __float_as_int(b[i]);
+  if (__any_sync(0xffffffffu, d != 0) && (threadIdx.x & 31) == 0) atomicExch(flag, 1);
+}
+
+cudaError_t launch_differs(const float* a, const float* b, size_t n, int* flag, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  differs_kernel<<<1216, 256, 0, st>>>(a, b, n, flag);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_norm_mask(const DevGeom& g, const float* proj_blank, const float* blank, float* calib,
                              cudaStream_t st) {
   const size_t n = (size_t)g.P * g.nang * g.nrad;

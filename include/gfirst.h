@@ -272,16 +272,22 @@ void gf_batch_destroy(gf_batch* b);
  * the kernels are launched directly, frame by frame.  Asynchronous. */
 gf_status gf_batch_iterate(gf_batch* b, int32_t n, int32_t use_graph);
 gf_status gf_batch_synchronize(gf_batch* b);
-/* With fused != 0, mode-1 frames that share geometry, subset count, storage,
- * filters, back-projector form and tile shapes advance as fused groups of up
- * to 16: every stage of a sub-iteration (forward PSF, projection + ratio,
- * back projection, update) is one kernel launch over the group's frames,
- * each frame keeping its own data and results (the same as alone).  Other
- * frames run on their own as before.  Takes effect at the next iterate. */
+/* With fused = 1 or 2, mode-1 frames that share geometry, subset count,
+ * storage, filters, back-projector form and tile shapes advance as fused
+ * groups of up to 16: every stage of a sub-iteration (forward PSF,
+ * projection + ratio, back projection, update) is one kernel launch over the
+ * group's frames, each frame keeping its own data and results (the same as
+ * alone, bit for bit).  With fused = 1, a group whose frames' normalization
+ * masks are equal (checked on the device) and whose back projector is in
+ * the per-view form back-projects two frames per warp, sharing the per-view
+ * geometry and the staged mask rows; fused = 2 keeps one frame per warp.
+ * Other frames run on their own.  0 turns fusing off.  Takes effect at the
+ * next iterate. */
 gf_status gf_batch_set_fused(gf_batch* b, int32_t fused);
-/* Units the batch runs (fused groups and single frames) and the size of the
- * largest group, as they stand now. */
-gf_status gf_batch_groups(gf_batch* b, int32_t* units, int32_t* largest);
+/* Units the batch runs (fused groups and single frames), the size of the
+ * largest group and the frame pairs back-projected together, as they stand
+ * now (waits for the frames' queued work to compare their masks). */
+gf_status gf_batch_groups(gf_batch* b, int32_t* units, int32_t* largest, int32_t* paired);
 
 /* ---- serving (no counterpart in the reference) ---------------------------- */
 /* Device bytes a reconstruction of these parameters holds (admission control). */

@@ -795,12 +795,14 @@ def test_batch_matches_frames_run_alone(gf, graph):
     b.close()
 
 
-@pytest.mark.parametrize("graph", [True, False])
-def test_fused_batch_matches_frames_run_alone(gf, graph):
+@pytest.mark.parametrize("graph,pairs", [(True, True), (False, True), (True, False)])
+def test_fused_batch_matches_frames_run_alone(gf, graph, pairs):
     """Fused groups (gf_batch_set_fused): the four mode-1 frames with two
-    subsets run every stage as one launch over the group; the frame with three
-    subsets and the mode-2 frame run on their own.  Every frame's images equal
-    the same frame run alone, bit for bit (the same arithmetic per frame)."""
+    subsets run every stage as one launch over the group (with pairs, their
+    back projection two frames per warp, the normalization being the same);
+    the frame with three subsets and the mode-2 frame run on their own.
+    Every frame's images equal the same frame run alone, bit for bit (the
+    same arithmetic per frame)."""
     d = parsed("tinyb")
     specs = [(1, 2), (1, 3), (1, 2), (2, 2), (1, 2), (1, 2)]
     frames = _frames(gf, specs)
@@ -819,8 +821,8 @@ def test_fused_batch_matches_frames_run_alone(gf, graph):
         a.iterate(3)
         alone.append((a.image(0), a.image(1)))
     b = gf.Batch([r for _, r in frames])
-    b.set_fused(True)
-    assert b.groups() == (3, 4)
+    b.set_fused(True, pairs=pairs)
+    assert b.groups() == (3, 4, 2 if pairs else 0)
     l0 = sum(c.launches() for c, _ in frames)
     b.iterate(1, graph=graph)
     b.iterate(2, graph=graph)
@@ -844,9 +846,9 @@ def test_fused_groups_hold_at_most_sixteen_frames(gf):
         r.load(dsino=np.roll(d["dsino"], k), norm=d["norm"])
         frames.append((c, r))
     b = gf.Batch([r for _, r in frames])
-    assert b.groups() == (18, 1)
+    assert b.groups() == (18, 1, 0)
     b.set_fused(True)
-    assert b.groups() == (2, 16)
+    assert b.groups() == (2, 16, 9)  # 8 pairs in the group of 16, 1 in the group of 2
     b.iterate(2, graph=True)
     b.sync()
     for k in (0, 15, 17):
@@ -856,6 +858,70 @@ def test_fused_groups_hold_at_most_sixteen_frames(gf):
         a.iterate(2)
         assert np.array_equal(frames[k][1].image(0), a.image(0)), k
     b.close()
+
+
+def test_fused_pairs_need_equal_normalizations(gf):
+    """Frames whose normalization masks differ are fused but not paired."""
+    d = parsed("tinyb")
+    g = gf.Geometry(*case("tinyb"))
+    frames = []
+    for k in range(3):
+        c = gf.Context(g, nsub=2)
+        r = gf.Recon(c, 1, niter=2)
+        norm = d["norm"].copy()
+        if k == 1:
+            norm[:: 5] = 0.0  # masks this frame's bins
+        r.load(dsino=d["dsino"], norm=norm)
+        frames.append((c, r, norm))
+    b = gf.Batch([r for _, r, _ in frames])
+    b.set_fused(True)
+    assert b.groups() == (1, 3, 0)
+    b.iterate(2)
+    b.sync()
+    for c, r, norm in frames:
+        c2 = gf.Context(g, nsub=2)
+        a = gf.Recon(c2, 1, niter=2)
+        a.load(dsino=d["dsino"], norm=norm)
+        a.iterate(2)
+        assert np.array_equal(r.image(0), a.image(0))
+    b.close()
+
+
+def test_fused_pairs_at_preclinical_size_match_frames_alone(gf):
+    """Three preclinical frames of one normalization, 16 subsets, FP32 and FP16
+    storage: a pair back-projected together and the third alone in the fused
+    group, against each frame run alone, bit for bit."""
+    g = gf.Geometry.preclinical()
+    P, ndata, nvox = gf.sizes(g)
+    rs = np.random.RandomState(5)
+    norm = rs.uniform(0.85, 1.15, ndata).astype(np.float32)
+    data = [np.concatenate([rs.poisson(lam, ndata), np.zeros(ndata)]).astype(np.float32) for lam in (2.0, 5.0, 9.0)]
+    for storage in ("f32", "f16"):
+        frames = []
+        for k in range(3):
+            c = gf.Context(g, nsub=16)
+            r = gf.Recon(c, 1, niter=1, storage=storage)
+            r.load(dsino=data[k], norm=norm)
+            frames.append((c, r))
+        b = gf.Batch([r for _, r in frames])
+        b.set_fused(True)
+        assert b.groups() == (1, 3, 1)
+        b.iterate(1)
+        b.sync()
+        got = [r.image(0) for _, r in frames]
+        b.close()
+        for _, r in frames:
+            r.close()
+        for c, _ in frames:
+            c.close()
+        for k in range(3):
+            c = gf.Context(g, nsub=16)
+            a = gf.Recon(c, 1, niter=1, storage=storage)
+            a.load(dsino=data[k], norm=norm)
+            a.iterate(1)
+            assert np.array_equal(got[k], a.image(0)), (storage, k)
+            a.close()
+            c.close()
 
 
 def test_batch_recaptures_after_retune_and_reload(gf):
