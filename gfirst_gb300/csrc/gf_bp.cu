@@ -338,7 +338,7 @@ __device__ __forceinline__ void voxel_window_pair(float2 (&accA)[Q], float2 (&ac
 }
 
 #ifndef GF_BP_PAIR_PF32
-#define GF_BP_PAIR_PF32 2
+#define GF_BP_PAIR_PF32 1
 #endif
 #ifndef GF_BP_PAIR_PF16
 #define GF_BP_PAIR_PF16 3
