@@ -1249,7 +1249,7 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference", "reference-shim"])
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-steps", type=int, default=12)
     ap.add_argument("--fp64-steps", type=int, default=4, help="sub-iterations of the FP64 oracle for the "
                     "headline's accuracy field (0: FP32 oracle only)")

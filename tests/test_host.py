@@ -45,7 +45,7 @@ def test_library_exports_every_declared_symbol(gf):
 
 
 def test_abi_version(gf):
-    assert gf.lib().gf_abi_version() == 2
+    assert gf.lib().gf_abi_version() == 3
 
 
 GEOS = [inputs.GEOMS["tiny"], inputs.GEOMS["tinyb"], inputs.GEOMS["small"],
