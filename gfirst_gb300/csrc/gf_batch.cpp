@@ -207,6 +207,7 @@ static gf_status capture(gf_batch* b) {
   for (size_t i = 0; i < b->frames.size(); i++) {
     prof[i] = b->frames[i]->prof;
     b->frames[i]->prof = false;  // no timing events inside the graph
+    b->frames[i]->marking = false;
     gf_ctx* c = b->frames[i]->ctx;
     if (std::find(ctxs.begin(), ctxs.end(), c) == ctxs.end()) {
       ctxs.push_back(c);
@@ -231,6 +232,7 @@ static gf_status capture(gf_batch* b) {
   // first of its frames
   for (size_t i = 0; i < b->frames.size(); i++) {
     b->frames[i]->prof = prof[i];
+    b->frames[i]->marking = true;
     b->frames[i]->launches_per_iteration = 0;
   }
   for (size_t k = 0; k < ctxs.size(); k++) {
@@ -285,8 +287,11 @@ gf_status gf_batch_iterate(gf_batch* b, int32_t n, int32_t use_graph) {
         GF_TRY(unit_iteration(b, ku));
         if (u.size() > 1) {
           GF_CK(cudaEventRecord(b->joins[u[0]], s0));
-          for (size_t k = 1; k < u.size(); k++)
+          b->frames[u[0]]->mark();
+          for (size_t k = 1; k < u.size(); k++) {
             GF_CK(cudaStreamWaitEvent(b->frames[u[k]]->ctx->stream, b->joins[u[0]], 0));
+            b->frames[u[k]]->mark();  // the group's work, seen from this frame's stream
+          }
         }
       }
     }
@@ -315,6 +320,7 @@ gf_status gf_batch_iterate(gf_batch* b, int32_t n, int32_t use_graph) {
   for (size_t i = 0; i < b->frames.size(); i++) {
     GF_CK(cudaEventRecord(b->joins[i], b->origin));
     GF_CK(cudaStreamWaitEvent(b->frames[i]->ctx->stream, b->joins[i], 0));
+    b->frames[i]->mark();
   }
   return GF_OK;
 }

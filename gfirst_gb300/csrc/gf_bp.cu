@@ -38,6 +38,24 @@
 
 namespace gf {
 
+// A column's results: its (NUMER, DENOM) sums, padding slices 0; or, with
+// `ratio`, the update ratio of the two alone in NUMER's buffer (padding
+// slices 1, the ratio of zero sums).
+template <int Q>
+__device__ __forceinline__ void store_column(const BpFrame& F, int ratio, size_t cb, int lane, int nzs,
+                                             const float2 (&acc)[Q]) {
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const int iz = lane + 32 * q;
+    if (ratio) {
+      F.numer[cb + iz] = iz < nzs ? update_ratio(acc[q].x, acc[q].y) : 1.f;
+    } else {
+      F.numer[cb + iz] = iz < nzs ? acc[q].x : 0.f;
+      F.denom[cb + iz] = iz < nzs ? acc[q].y : 0.f;
+    }
+  }
+}
+
 // a - b on packed pairs, each element rounded as the scalar subtraction
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) {
   float2 c;
@@ -277,14 +295,7 @@ __device__ __forceinline__ void bp_column(const BpArgs& a, int rmax) {
 #undef GF_SEG
     }
   }
-  float* no = F.numer + (size_t)colidx * g.nzp;
-  float* dO = F.denom + (size_t)colidx * g.nzp;
-#pragma unroll
-  for (int q = 0; q < Q; q++) {
-    const int iz = lane + 32 * q;
-    no[iz] = iz < g.nzs ? acc[q].x : 0.f;
-    dO[iz] = iz < g.nzs ? acc[q].y : 0.f;
-  }
+  store_column<Q>(F, a.ratio, (size_t)colidx * g.nzp, lane, g.nzs, acc);
 }
 
 // ---- two frames per warp ------------------------------------------------
@@ -478,14 +489,8 @@ __device__ __forceinline__ void bp_column_pair(const BpArgs& a, int rmax) {
     }
   }
   const size_t cb = (size_t)colidx * g.nzp;
-#pragma unroll
-  for (int q = 0; q < Q; q++) {
-    const int iz = lane + 32 * q;
-    FA.numer[cb + iz] = iz < g.nzs ? accA[q].x : 0.f;
-    FA.denom[cb + iz] = iz < g.nzs ? accA[q].y : 0.f;
-    FB.numer[cb + iz] = iz < g.nzs ? accB[q].x : 0.f;
-    FB.denom[cb + iz] = iz < g.nzs ? accB[q].y : 0.f;
-  }
+  store_column<Q>(FA, a.ratio, cb, lane, g.nzs, accA);
+  store_column<Q>(FB, a.ratio, cb, lane, g.nzs, accB);
 }
 
 #ifndef GF_BP_PAIR_REGS
@@ -506,7 +511,7 @@ cudaError_t launch_bp_pairs(const BpArgs& a, int warps, cudaStream_t st) {
   const int npairs = a.nfr / 2;
   if (npairs < 1 || 2 * npairs != a.nfr || a.nfr > kMaxFrames) return cudaErrorInvalidValue;
   for (int f = 0; f < a.nfr; f++)
-    if (!a.fr[f].corrcal || !a.fr[f].numer || !a.fr[f].denom) return cudaErrorInvalidValue;
+    if (!a.fr[f].corrcal || !a.fr[f].numer || (!a.ratio && !a.fr[f].denom)) return cudaErrorInvalidValue;
   const int Q = a.g.nzp / 32;
   const int rmax = a.rbuf;
   dim3 grid((a.g.res * a.g.res + warps - 1) / warps, npairs);
@@ -578,7 +583,7 @@ cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st) {
   const int rmax = a.fast ? a.rbuf : a.g.nzs + 2;
   if (a.nfr < 0 || a.nfr > kMaxFrames) return cudaErrorInvalidValue;
   for (int f = 0; f < (a.nfr > 1 ? a.nfr : 1); f++)
-    if (!a.fr[f].corrcal || !a.fr[f].numer || !a.fr[f].denom) return cudaErrorInvalidValue;
+    if (!a.fr[f].corrcal || !a.fr[f].numer || (!a.ratio && !a.fr[f].denom)) return cudaErrorInvalidValue;
   dim3 grid((a.g.res * a.g.res + warps - 1) / warps, a.nfr > 1 ? a.nfr : 1);
   size_t smem = (size_t)warps * (a.na * sizeof(int4) + rmax * sizeof(float2));
   void (*k)(BpArgs, int) = nullptr;

@@ -267,6 +267,8 @@ gf_status gf_create(const gf_geometry* g, int32_t nsubsets, int32_t device, gf_c
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(cuda_error(cudaGetLastError(), "cudaStreamCreate"));
   c->own_stream = true;
+  if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(cuda_error(cudaGetLastError(), "cudaStreamCreate (copies)"));
   const Plan& p = c->plan;
   std::vector<DevSeg> segs(p.g.nseg);
   for (int s = 0; s < p.g.nseg; s++)
@@ -324,6 +326,10 @@ void gf_destroy(gf_ctx* c) {
   cudaStreamSynchronize(fs);
   if (fs) cudaStreamDestroy(fs);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
   delete c;
 }
 
@@ -492,7 +498,7 @@ gf_status gf_psf_xy(gf_ctx* c, const float* d_in, float psf, float* d_out) {
   if (!c || !d_in || !d_out) return set_error(GF_ERR_ARG, "null argument");
   GF_TRY(c->ensure_scratch());
   GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_in, c->s_img, c->stream));
-  GF_LAUNCH(c, launch_conv_xy(c->dg, c->s_img, nullptr, gauss9(psf), c->s_img2, c->stream));
+  GF_LAUNCH(c, launch_conv_xy(c->dg, c->s_img, gauss9(psf), c->s_img2, c->stream));
   GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_img2, 1.f, 0, d_out, c->stream));
   return GF_OK;
 }
@@ -503,8 +509,8 @@ gf_status gf_image_update(gf_ctx* c, float* d_image, const float* d_numer, const
   GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_numer, c->s_numer, c->stream));
   GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_denom, c->s_denom, c->stream));
   GF_LAUNCH(c, launch_file_to_zfast(c->dg, d_image, c->s_img, c->stream));
-  GF_LAUNCH(c, launch_conv_xy(c->dg, c->s_numer, c->s_denom, gauss9(psf_bw), c->s_img2, c->stream));
-  GF_LAUNCH(c, launch_zfilter_update(c->dg, c->s_img2, gauss5(), c->s_img, c->stream));
+  GF_LAUNCH(c, launch_voxel_ratio(c->dg, c->s_numer, c->s_denom, c->s_img2, c->stream));
+  GF_LAUNCH(c, launch_update(c->dg, c->s_img2, gauss9(psf_bw), gauss5(), c->s_img, c->stream));
   GF_LAUNCH(c, launch_zfast_to_file(c->dg, c->s_img, 1.f, 0, d_image, c->stream));
   return GF_OK;
 }

@@ -40,6 +40,9 @@ template <> __device__ __forceinline__ __nv_bfloat162 pair_from<__nv_bfloat162>(
 
 __device__ __forceinline__ float lerp_rn(float a, float b, float w) { return __fmaf_rn(w, __fsub_rn(b, a), a); }
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
+// The update ratio of divVxVGPU (GFIRST_GPU_Kernels.cu:173-182): NUMER/DENOM,
+// 1 where DENOM < 0.001.
+__device__ __forceinline__ float update_ratio(float n, float d) { return d < 0.001f ? 1.0f : __fdiv_rn(n, d); }
 
 // Angle index of the l-th angle of subset s.
 __device__ __forceinline__ int subset_angle(const DevGeom& g, int s, int l) { return s + l * g.nsub; }

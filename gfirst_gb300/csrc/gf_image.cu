@@ -1,7 +1,8 @@
 // gf_image.cu -- image-domain kernels on z-fast volumes [RES][RES][NZP].
 //
 // The update chain of GFIRST.cu:482-502 (divVxVGPU, convolutionXY,
-// gaussian_filterZ, multiply, edge-slice copy), the forward PSF
+// gaussian_filterZ, multiply, edge-slice copy; the back projector writes the
+// ratio, the rest is one kernel), the forward PSF
 // (GFIRST.cu:324-340), the joint bilateral filter (GFIRST_GPU_Kernels.cu:
 // 508-539) and layout conversions.  All of these are HBM-bound except the
 // bilateral filter; they keep the reference's operation order with explicit
@@ -20,57 +21,12 @@ __device__ __forceinline__ void img_st(__half* p, float v) { *p = __float2half_r
 __device__ __forceinline__ void img_st(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
 
 // ---- separable XY Gaussian, GFIRST_GPU_Kernels.cu:332-358 -----------------
-// CTA: 8x8 columns x 32 slices.  The y pass is zero-padded; the x pass runs
-// only for 3 < x < RES-4 and border columns output the raw input.  With DIV
-// the input is the update ratio numer/denom (1 where denom < 0.001,
-// divVxVGPU, GFIRST_GPU_Kernels.cu:173-182), computed on the fly.
-// Grid z runs over (frame, 32-slice chunk): frame f's buffers are fr.fr[f].
-template <bool DIV, class T>
-__global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const ImgFrames fr, const Taps9 G) {
-  __shared__ float S[16][16][32];
-  const int nzc = g.nzp / 32;
-  const int f = blockIdx.z / nzc;
-  const T* __restrict__ in = static_cast<const T*>(fr.fr[f].in);
-  const float* __restrict__ den = fr.fr[f].den;
-  float* __restrict__ out = fr.fr[f].out;
-  const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int x0 = blockIdx.x * 8, y0 = blockIdx.y * 8, z = (blockIdx.z - f * nzc) * 32 + lane;
-  const int RES = g.res, NZP = g.nzp;
-  if (!DIV) {
-#pragma unroll 8
-    for (int c = ty; c < 256; c += 8) {
-      const int yy = c >> 4, xx = c & 15;
-      const int y = y0 - 4 + yy, x = x0 - 4 + xx;
-      S[yy][xx][lane] = (y >= 0 && y < RES && x >= 0 && x < RES) ? img_ld(in + ((size_t)y * RES + x) * NZP + z) : 0.f;
-    }
-  }
-  // with DIV, batches of eight columns: every load of a batch is issued before
-  // any division (the IEEE division's slow path is a call, which keeps the
-  // compiler from moving loads across it), so each warp has 16 loads in flight
-  // instead of one or two (67 -> 32 us at the preclinical size)
-#pragma unroll 1
-  for (int c0 = ty; DIV && c0 < 256; c0 += 64) {
-    float nv[8], dv[8];
-    size_t o[8];
-    bool ok[8];
-#pragma unroll
-    for (int u = 0; u < 8; u++) {
-      const int c = c0 + 8 * u;
-      const int y = y0 - 4 + (c >> 4), x = x0 - 4 + (c & 15);
-      ok[u] = y >= 0 && y < RES && x >= 0 && x < RES;
-      o[u] = ok[u] ? ((size_t)y * RES + x) * NZP + z : 0;
-      nv[u] = ok[u] ? img_ld(in + o[u]) : 0.f;
-      if (DIV) dv[u] = ok[u] ? den[o[u]] : 1.f;
-    }
-#pragma unroll
-    for (int u = 0; u < 8; u++) {
-      const int c = c0 + 8 * u;
-      float v = nv[u];
-      if (DIV && ok[u]) v = (dv[u] < 0.001f) ? 1.0f : __fdiv_rn(nv[u], dv[u]);
-      S[c >> 4][c & 15][lane] = v;
-    }
-  }
-  __syncthreads();
+// conv_xy9 runs it on an 8x8-column, 32-slice tile staged with a 4-column
+// halo in S: the y pass is zero-padded; the x pass runs only for
+// 3 < x < RES-4 and border columns output the raw input.  Thread (row ty,
+// lane) leaves the 8 outputs of its row at its slice in v[].
+__device__ __forceinline__ void conv_xy9(float (&S)[16][16][32], int ty, int lane, int x0, int RES, const Taps9& G,
+                                         float (&v)[8]) {
   // the y pass of row ty over the 16 halo columns stays in this thread's
   // registers: the x pass below reads only its own row and slice
   float yv[16];
@@ -81,162 +37,188 @@ __global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const Img
     for (int k = 1; k < 9; k++) acc = __fadd_rn(acc, __fmul_rn(S[ty + k][xx][lane], G.c[k]));
     yv[xx] = acc;
   }
+#pragma unroll
+  for (int xo = 0; xo < 8; xo++) {
+    const int x = x0 + xo;
+    if (x > 3 && x < RES - 4) {
+      float a = __fmul_rn(yv[xo], G.c[0]);
+#pragma unroll
+      for (int k = 1; k < 9; k++) a = __fadd_rn(a, __fmul_rn(yv[xo + k], G.c[k]));
+      v[xo] = a;
+    } else {
+      v[xo] = S[ty + 4][xo + 4][lane];
+    }
+  }
+}
+
+// The forward PSF (GFIRST.cu:324-340) of an image.  CTA: 8x8 columns x 32
+// slices; grid z runs over (frame, 32-slice chunk): frame f's buffers are
+// fr.fr[f].
+template <class T>
+__global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const ImgFrames fr, const Taps9 G) {
+  __shared__ float S[16][16][32];
+  const int nzc = g.nzp / 32;
+  const int f = blockIdx.z / nzc;
+  const T* __restrict__ in = static_cast<const T*>(fr.fr[f].in);
+  float* __restrict__ out = fr.fr[f].out;
+  const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int x0 = blockIdx.x * 8, y0 = blockIdx.y * 8, z = (blockIdx.z - f * nzc) * 32 + lane;
+  const int RES = g.res, NZP = g.nzp;
+#pragma unroll 8
+  for (int c = ty; c < 256; c += 8) {
+    const int yy = c >> 4, xx = c & 15;
+    const int y = y0 - 4 + yy, x = x0 - 4 + xx;
+    S[yy][xx][lane] = (y >= 0 && y < RES && x >= 0 && x < RES) ? img_ld(in + ((size_t)y * RES + x) * NZP + z) : 0.f;
+  }
+  __syncthreads();
+  float v[8];
+  conv_xy9(S, ty, lane, x0, RES, G, v);
   const int y = y0 + ty;
   if (y >= RES) return;
 #pragma unroll
   for (int xo = 0; xo < 8; xo++) {
     const int x = x0 + xo;
     if (x >= RES) break;
-    float v;
-    if (x > 3 && x < RES - 4) {
-      v = __fmul_rn(yv[xo], G.c[0]);
-#pragma unroll
-      for (int k = 1; k < 9; k++) v = __fadd_rn(v, __fmul_rn(yv[xo + k], G.c[k]));
-    } else {
-      v = S[ty + 4][xo + 4][lane];
-    }
-    out[((size_t)y * RES + x) * NZP + z] = (z < g.nzs) ? v : 0.f;
+    out[((size_t)y * RES + x) * NZP + z] = (z < g.nzs) ? v[xo] : 0.f;
   }
 }
 
-cudaError_t launch_conv_xy_frames(const DevGeom& g, const ImgFrames& f, int nfr, bool div, const Taps9& t,
-                                  cudaStream_t st, int in_store) {
+cudaError_t launch_conv_xy_frames(const DevGeom& g, const ImgFrames& f, int nfr, const Taps9& t, cudaStream_t st,
+                                  int in_store) {
   if (nfr < 1 || nfr > kMaxFrames) return cudaErrorInvalidValue;
   for (int k = 0; k < nfr; k++)
-    if (!f.fr[k].in || !f.fr[k].out || (div && !f.fr[k].den)) return cudaErrorInvalidValue;
+    if (!f.fr[k].in || !f.fr[k].out) return cudaErrorInvalidValue;
   dim3 grid((g.res + 7) / 8, (g.res + 7) / 8, (g.nzp / 32) * nfr);
-  if (div) {
-    if (in_store != 0) return cudaErrorInvalidValue;
-    conv_xy_kernel<true, float><<<grid, 256, 0, st>>>(g, f, t);
-  } else if (in_store == 1) {
-    conv_xy_kernel<false, __half><<<grid, 256, 0, st>>>(g, f, t);
+  if (in_store == 1) {
+    conv_xy_kernel<__half><<<grid, 256, 0, st>>>(g, f, t);
   } else if (in_store == 2) {
-    conv_xy_kernel<false, __nv_bfloat16><<<grid, 256, 0, st>>>(g, f, t);
+    conv_xy_kernel<__nv_bfloat16><<<grid, 256, 0, st>>>(g, f, t);
   } else {
-    conv_xy_kernel<false, float><<<grid, 256, 0, st>>>(g, f, t);
+    conv_xy_kernel<float><<<grid, 256, 0, st>>>(g, f, t);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_conv_xy(const DevGeom& g, const void* in, const float* den, const Taps9& t, float* out,
-                           cudaStream_t st, int in_store) {
+cudaError_t launch_conv_xy(const DevGeom& g, const void* in, const Taps9& t, float* out, cudaStream_t st,
+                           int in_store) {
   ImgFrames f{};
   f.fr[0].in = in;
-  f.fr[0].den = den;
   f.fr[0].out = out;
-  return launch_conv_xy_frames(g, f, 1, den != nullptr, t, st, in_store);
+  return launch_conv_xy_frames(g, f, 1, t, st, in_store);
+}
+
+// ---- the update ratio, divVxVGPU (GFIRST_GPU_Kernels.cu:173-182) ------------
+__global__ void __launch_bounds__(256) voxel_ratio_kernel(size_t n, const float* __restrict__ numer,
+                                                          const float* __restrict__ denom, float* __restrict__ out) {
+  const size_t i = (size_t)blockIdx.x * 256 + threadIdx.x;
+  if (i < n) out[i] = update_ratio(numer[i], denom[i]);
+}
+
+cudaError_t launch_voxel_ratio(const DevGeom& g, const float* numer, const float* denom, float* out,
+                               cudaStream_t st) {
+  const size_t n = (size_t)g.res * g.res * g.nzp;
+  voxel_ratio_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, numer, denom, out);
+  return cudaGetLastError();
 }
 
 // ---- axial filter, gaussian_filterZ (GFIRST_CPU_Kernels.cpp:165-187) -------
 // Its loop counter is incremented before use, so loop position (K, y, x)
 // writes voxel (K, y, x)+1: voxel (z, y, x) takes the rule of slice z, except
 // column (y=0, x=0), which takes the rule of slice z-1; reads past the last
-// slice are 0.  The rule is applied centred on the voxel itself.
-__device__ __forceinline__ float zrule(const float* c, int ze, int K, int NZS, const Taps5 g) {
-  auto in = [&](int zz) { return (zz >= 0 && zz < NZS) ? c[zz] : 0.f; };
-  if (K == 0) return __fadd_rn(__fmul_rn(0.5f, in(ze)), __fmul_rn(0.5f, in(ze + 1)));
-  if (K == NZS - 1) return __fadd_rn(__fmul_rn(0.5f, in(ze - 1)), __fmul_rn(0.5f, in(ze)));
+// slice are 0.  The rule is applied centred on the voxel itself; m2..p2 are
+// the inputs at slices z-2..z+2, already 0 outside [0, NZS).
+__device__ __forceinline__ float zrule(float m2, float m1, float c0, float p1, float p2, int K, int NZS,
+                                       const Taps5& g) {
+  if (K == 0) return __fadd_rn(__fmul_rn(0.5f, c0), __fmul_rn(0.5f, p1));
+  if (K == NZS - 1) return __fadd_rn(__fmul_rn(0.5f, m1), __fmul_rn(0.5f, c0));
   if (K == 1 || K == NZS - 2)
-    return __fadd_rn(__fadd_rn(__fmul_rn(0.333f, in(ze - 1)), __fmul_rn(0.333f, in(ze))), __fmul_rn(0.333f, in(ze + 1)));
-  float v = __fmul_rn(g.c[0], in(ze - 2));
-  v = __fadd_rn(v, __fmul_rn(g.c[1], in(ze - 1)));
-  v = __fadd_rn(v, __fmul_rn(g.c[2], in(ze)));
-  v = __fadd_rn(v, __fmul_rn(g.c[3], in(ze + 1)));
-  v = __fadd_rn(v, __fmul_rn(g.c[4], in(ze + 2)));
+    return __fadd_rn(__fadd_rn(__fmul_rn(0.333f, m1), __fmul_rn(0.333f, c0)), __fmul_rn(0.333f, p1));
+  float v = __fmul_rn(g.c[0], m2);
+  v = __fadd_rn(v, __fmul_rn(g.c[1], m1));
+  v = __fadd_rn(v, __fmul_rn(g.c[2], c0));
+  v = __fadd_rn(v, __fmul_rn(g.c[3], p1));
+  v = __fadd_rn(v, __fmul_rn(g.c[4], p2));
   return v;
 }
 
-// img = img * factor, then slice 0 <- slice 1 and slice NZS-1 <- slice
-// NZS-2 (GFIRST.cu:492-496), in place.  One warp owns a column and reads all
-// of its slices before writing any, so the edge slices see the column's old
-// values as the reference's multiply-then-copy order requires.  Voxel 0's
-// factor (DENOM[0] in the reference) only reaches slice 0, which the edge
-// copy overwrites.
-// Grid y runs over frames: frame f's C is fr.fr[f].out, its image fr.fr[f].img.
-template <int Q, class T>
-__global__ void __launch_bounds__(256) zfilter_update_kernel(const DevGeom g, const ImgFrames fr, const Taps5 t5) {
-  const float* __restrict__ C = fr.fr[blockIdx.y].out;
-  T* img = static_cast<T*>(fr.fr[blockIdx.y].img);
-  const int lane = threadIdx.x & 31;
-  const int colidx = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (colidx >= g.res * g.res) return;  // whole warp
-  const size_t cb = (size_t)colidx * g.nzp;
-  const int NZS = g.nzs;
-  float v[Q];
-#pragma unroll
-  for (int q = 0; q < Q; q++) v[q] = img_ld(img + cb + lane + 32 * q);
-  const float s1 = __shfl_sync(0xffffffffu, v[0], 1);
-  float sl = 0.f;
-#pragma unroll
-  for (int q = 0; q < Q; q++) {
-    const float w = __shfl_sync(0xffffffffu, v[q], (NZS - 2) & 31);
-    if (q == (NZS - 2) >> 5) sl = w;
-  }
-#pragma unroll
-  for (int q = 0; q < Q; q++) {
-    const int z = lane + 32 * q;
-    float out = 0.f;
-    if (z < NZS) {
-      const int ze = (z == 0) ? 1 : (z == NZS - 1 ? NZS - 2 : z);
-      const float iv = (z == 0) ? s1 : (z == NZS - 1 ? sl : v[q]);
-      const int K = (colidx == 0) ? ze - 1 : ze;
-      out = __fmul_rn(iv, zrule(C + cb, ze, K, NZS, t5));
-    }
-    img_st(img + cb + z, out);
-  }
-}
-
+// ---- the image update of GFIRST.cu:482-496 in one pass ----------------------
+// C = convolutionXY(ratio), img = img * gaussian_filterZ(C), then slice 0 <-
+// slice 1 and slice NZS-1 <- slice NZS-2, in place.  CTA: 8x8 columns x `cs`
+// output slices from z0; lane l holds slice z0 - 2 + l, so C is computed on
+// the chunk and two slices either side (lanes 2..cs+1 are the outputs) and
+// the axial taps are register shuffles of C.  The edge copies take the
+// neighbour slice's old image value and rule, i.e. the neighbour's updated
+// value: a shuffle of the products.  Slice 1 always sits in slice 0's chunk,
+// and `cs` is chosen so that slice NZS-1 is never a chunk's first output, so
+// a CTA reads image values of its own outputs only and the in-place update
+// needs no ordering between CTAs.  Grid z runs over (frame, chunk).
 template <class T>
-static cudaError_t zfilter_update_t(const DevGeom& g, const ImgFrames& f, int nfr, const Taps5& t5, cudaStream_t st) {
-  dim3 grid((g.res * g.res + 7) / 8, nfr);
-  switch (g.nzp / 32) {
-#define GF_ZF(QQ) \
-  case QQ: zfilter_update_kernel<QQ, T><<<grid, 256, 0, st>>>(g, f, t5); break;
-    GF_ZF(1) GF_ZF(2) GF_ZF(3) GF_ZF(4) GF_ZF(5) GF_ZF(6) GF_ZF(7) GF_ZF(8)
-#undef GF_ZF
-    default: return cudaErrorInvalidValue;
+__global__ void __launch_bounds__(256) update_kernel(const DevGeom g, const ImgFrames fr, const Taps9 G,
+                                                     const Taps5 t5, int cs) {
+  __shared__ float S[16][16][32];
+  const int nzc = (g.nzp + cs - 1) / cs;
+  const int f = blockIdx.z / nzc;
+  const float* __restrict__ ratio = static_cast<const float*>(fr.fr[f].in);
+  T* img = static_cast<T*>(fr.fr[f].img);
+  const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int x0 = blockIdx.x * 8, y0 = blockIdx.y * 8;
+  const int z = (blockIdx.z - f * nzc) * cs - 2 + lane;
+  const int RES = g.res, NZP = g.nzp, NZS = g.nzs;
+  const bool zload = z >= 0 && z < NZP;
+#pragma unroll 8
+  for (int c = ty; c < 256; c += 8) {
+    const int yy = c >> 4, xx = c & 15;
+    const int y = y0 - 4 + yy, x = x0 - 4 + xx;
+    S[yy][xx][lane] = (zload && y >= 0 && y < RES && x >= 0 && x < RES) ? ratio[((size_t)y * RES + x) * NZP + z] : 0.f;
   }
-  return cudaGetLastError();
+  __syncthreads();
+  float v[8];
+  conv_xy9(S, ty, lane, x0, RES, G, v);
+  const int y = y0 + ty;
+  if (y >= RES) return;  // whole warp
+  const bool out_lane = lane >= 2 && lane < cs + 2 && z < NZP;
+  const bool zin = z >= 0 && z < NZS;
+#pragma unroll
+  for (int xo = 0; xo < 8; xo++) {
+    const int x = x0 + xo;
+    if (x >= RES) break;  // whole warp
+    const size_t o = ((size_t)y * RES + x) * NZP + z;
+    const float iv = out_lane ? img_ld(img + o) : 0.f;
+    const float c0 = zin ? v[xo] : 0.f;
+    const float m1 = __shfl_up_sync(0xffffffffu, c0, 1), m2 = __shfl_up_sync(0xffffffffu, c0, 2);
+    const float p1 = __shfl_down_sync(0xffffffffu, c0, 1), p2 = __shfl_down_sync(0xffffffffu, c0, 2);
+    const int K = (x == 0 && y == 0) ? z - 1 : z;
+    const float prod = __fmul_rn(iv, zrule(m2, m1, c0, p1, p2, K, NZS, t5));
+    const float up = __shfl_down_sync(0xffffffffu, prod, 1);  // slice z + 1
+    const float dn = __shfl_up_sync(0xffffffffu, prod, 1);    // slice z - 1
+    if (out_lane) img_st(img + o, z >= NZS ? 0.f : (z == 0 ? up : (z == NZS - 1 ? dn : prod)));
+  }
 }
 
-cudaError_t launch_zfilter_update_frames(const DevGeom& g, const ImgFrames& f, int nfr, const Taps5& t5,
-                                         cudaStream_t st, int img_store) {
+int update_chunk(const DevGeom& g) { return (g.nzs > 1 && (g.nzs - 1) % 28 == 0) ? 27 : 28; }
+
+cudaError_t launch_update_frames(const DevGeom& g, const ImgFrames& f, int nfr, const Taps9& t9, const Taps5& t5,
+                                 cudaStream_t st, int img_store) {
   if (nfr < 1 || nfr > kMaxFrames) return cudaErrorInvalidValue;
   for (int k = 0; k < nfr; k++)
-    if (!f.fr[k].out || !f.fr[k].img) return cudaErrorInvalidValue;
+    if (!f.fr[k].in || !f.fr[k].img) return cudaErrorInvalidValue;
+  const int cs = update_chunk(g);
+  dim3 grid((g.res + 7) / 8, (g.res + 7) / 8, ((g.nzp + cs - 1) / cs) * nfr);
   switch (img_store) {
-    case 0: return zfilter_update_t<float>(g, f, nfr, t5, st);
-    case 1: return zfilter_update_t<__half>(g, f, nfr, t5, st);
-    case 2: return zfilter_update_t<__nv_bfloat16>(g, f, nfr, t5, st);
+    case 0: update_kernel<float><<<grid, 256, 0, st>>>(g, f, t9, t5, cs); break;
+    case 1: update_kernel<__half><<<grid, 256, 0, st>>>(g, f, t9, t5, cs); break;
+    case 2: update_kernel<__nv_bfloat16><<<grid, 256, 0, st>>>(g, f, t9, t5, cs); break;
     default: return cudaErrorInvalidValue;
   }
-}
-
-cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const Taps5& t5, void* img, cudaStream_t st,
-                                  int img_store) {
-  ImgFrames f{};
-  f.fr[0].out = const_cast<float*>(C);
-  f.fr[0].img = img;
-  return launch_zfilter_update_frames(g, f, 1, t5, st, img_store);
-}
-
-// The axial filter on its own (voxel 0 keeps the value already in `out`).
-__global__ void __launch_bounds__(256) zfilter_kernel(const DevGeom g, const float* __restrict__ C, const Taps5 t5,
-                                                      float* __restrict__ out) {
-  const int lane = threadIdx.x & 31;
-  const int colidx = blockIdx.x * 8 + (threadIdx.x >> 5);
-  const int z = blockIdx.y * 32 + lane;
-  if (colidx >= g.res * g.res || z >= g.nzs) return;
-  if (colidx == 0 && z == 0) return;
-  const size_t cb = (size_t)colidx * g.nzp;
-  const int K = (colidx == 0) ? z - 1 : z;
-  out[cb + z] = zrule(C + cb, z, K, g.nzs, t5);
-}
-
-cudaError_t launch_zfilter(const DevGeom& g, const float* C, const Taps5& t5, float* out, cudaStream_t st) {
-  dim3 grid((g.res * g.res + 7) / 8, g.nzp / 32);
-  zfilter_kernel<<<grid, 256, 0, st>>>(g, C, t5, out);
   return cudaGetLastError();
+}
+
+cudaError_t launch_update(const DevGeom& g, const float* ratio, const Taps9& t9, const Taps5& t5, void* img,
+                          cudaStream_t st, int img_store) {
+  ImgFrames f{};
+  f.fr[0].in = ratio;
+  f.fr[0].img = img;
+  return launch_update_frames(g, f, 1, t9, t5, st, img_store);
 }
 
 // ---- layout conversion ------------------------------------------------------

@@ -54,6 +54,7 @@ struct gf_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  cudaStream_t copy_stream = nullptr;  // host-to-device uploads of loads (overlap the compute stream)
   std::vector<gf::DevBuf> owned;  // freed on destroy
   std::vector<gf_recon*> recons;  // reconstructions still open on this context (destroyed with it)
   gf::DevSeg* d_seg = nullptr;
@@ -98,9 +99,7 @@ struct gf_recon {
   // element type of image t: image_storage, except mode 1's unused triples image (FP32)
   int store(int t) const { return (t == 0 || p.mode >= 2) ? p.image_storage : GF_STORE_F32; }
   float* psf = nullptr;
-  float* numer = nullptr;
-  float* denom = nullptr;
-  float* ctmp = nullptr;
+  float* ratio = nullptr;  // the back projector's update ratio NUMER/DENOM, z-fast
   float* filt = nullptr;
   void* corrcal = nullptr;  // (ratio, mask) pairs of the current subset, gf_recon_params::storage
   float2* dbg[2] = {nullptr, nullptr};
@@ -116,6 +115,14 @@ struct gf_recon {
   float* datos_v = nullptr;
   float* d_max = nullptr;
   float* stage = nullptr;  // device staging of host inputs (3*NDATA floats)
+  cudaEvent_t ev_last = nullptr;        // the last work queued for this reconstruction (compute stream)
+  bool marking = true;                  // off while a batch captures this reconstruction's work
+  void mark() {
+    if (ev_last && marking) cudaEventRecord(ev_last, ctx->stream);
+  }
+  cudaEvent_t ev_staged = nullptr;      // the uploads into `stage` are done (copy stream)
+  cudaEvent_t ev_stage_free = nullptr;  // the layout kernels have read `stage` (compute stream)
+  bool stage_used = false;
   gf::Taps9 g_fw{}, g_bw{};
   gf::Taps5 g5{};
   int iters_done = 0;

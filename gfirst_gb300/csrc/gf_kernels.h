@@ -59,6 +59,9 @@ struct BpArgs {
   // oracle's sums bit for bit), 1 per view (BpPads; within 1e-5 of it).
   int fast;
   int pad_lo, rbuf;        // fast form: staged-row buffer per warp (BpPads)
+  // 0: write the column sums to BpFrame::numer and ::denom; 1: write the
+  // update ratio NUMER/DENOM (divVxVGPU) to ::numer alone (::denom unused).
+  int ratio;
 };
 cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st);
 // Per-view form over a.nfr = 2n frames as n pairs (frames 2p, 2p + 1) that
@@ -81,29 +84,32 @@ inline cudaError_t allow_max_smem(K k) {
 
 
 // ---- image kernels (gf_image.cu) ----
-// out = XY PSF of `in`; with `den` the input is the update ratio in/den.
-cudaError_t launch_conv_xy(const DevGeom& g, const void* in, const float* den, const Taps9& t, float* out,
-                           cudaStream_t st, int in_store = 0);
-// img *= axial_filter(C), then the edge-slice copy; in place.
-// img elements: in_store/img_store/out_store 0 FP32, 1 FP16, 2 BF16 (16-bit image storage)
-cudaError_t launch_zfilter_update(const DevGeom& g, const float* C, const Taps5& t5, void* img, cudaStream_t st,
-                                  int img_store = 0);
+// Image elements: in_store/img_store/out_store 0 FP32, 1 FP16, 2 BF16 (16-bit image storage).
+// out = XY PSF of the image `in`.
+cudaError_t launch_conv_xy(const DevGeom& g, const void* in, const Taps9& t, float* out, cudaStream_t st,
+                           int in_store = 0);
+// out = the update ratio NUMER/DENOM (1 where DENOM < 0.001), z-fast.
+cudaError_t launch_voxel_ratio(const DevGeom& g, const float* numer, const float* denom, float* out,
+                               cudaStream_t st);
+// img *= axial_filter(XY PSF of the update ratio), then the edge-slice copy;
+// in place, one launch.
+cudaError_t launch_update(const DevGeom& g, const float* ratio, const Taps9& t9, const Taps5& t5, void* img,
+                          cudaStream_t st, int img_store = 0);
 // The same two over nfr frames of one geometry in one launch each.
 struct ImgFrame {
-  const void* in;   // conv_xy input (image, or NUMER with den)
-  const float* den; // conv_xy: DENOM of the update ratio, or null
-  float* out;       // conv_xy output; the zfilter's C
-  void* img;        // zfilter_update: the image updated in place
+  const void* in;  // conv_xy: the image; update: the ratio (FP32)
+  float* out;      // conv_xy output
+  void* img;       // update: the image updated in place
 };
 struct ImgFrames {
   ImgFrame fr[kMaxFrames];
 };
-cudaError_t launch_conv_xy_frames(const DevGeom& g, const ImgFrames& f, int nfr, bool div, const Taps9& t,
-                                  cudaStream_t st, int in_store = 0);
-cudaError_t launch_zfilter_update_frames(const DevGeom& g, const ImgFrames& f, int nfr, const Taps5& t5,
-                                         cudaStream_t st, int img_store = 0);
-// Axial filter alone, z-fast in/out (voxel 0 keeps out's value).
-cudaError_t launch_zfilter(const DevGeom& g, const float* C, const Taps5& t5, float* out, cudaStream_t st);
+cudaError_t launch_conv_xy_frames(const DevGeom& g, const ImgFrames& f, int nfr, const Taps9& t, cudaStream_t st,
+                                  int in_store = 0);
+cudaError_t launch_update_frames(const DevGeom& g, const ImgFrames& f, int nfr, const Taps9& t9, const Taps5& t5,
+                                 cudaStream_t st, int img_store = 0);
+// Output slices per CTA of the update kernel.
+int update_chunk(const DevGeom& g);
 cudaError_t launch_file_to_zfast(const DevGeom& g, const float* in, float* out, cudaStream_t st);
 cudaError_t launch_zfast_to_file(const DevGeom& g, const void* in, float scale, int mask, float* out,
                                  cudaStream_t st, int in_store = 0);

@@ -14,11 +14,10 @@
 //
 // The array's name in host code is a host-side stand-in, not a device
 // address, so its device address is taken with cudaGetSymbolAddress once per
-// device, with that device current, on the first call on that device.  That
-// first call should come before any stream capture.  All calls share the one
-// array and it keeps the last call's contents; every call rewrites what it
-// reads before reading it.  Calls whose work overlaps on the GPU (different
-// streams, or another host thread) race on the array.
+// device, with that device current, on the first call on that device.  All
+// calls share the one array and it keeps the last call's contents; every call
+// rewrites what it reads before reading it.  Calls whose work overlaps on the
+// GPU (different streams, or another host thread) race on the array.
 #include <cstring>
 #include <mutex>
 #include <vector>

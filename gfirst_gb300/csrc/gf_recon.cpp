@@ -78,7 +78,7 @@ gf_status gf_recon::init_images() {
   GF_LAUNCH(c, launch_cylinder(c->dg, 1.0f, img[0], st, store(0)));
   GF_LAUNCH(c, launch_cylinder(c->dg, p.mode == 1 ? 0.0f : 1.0f, img[1], st, store(1)));
   if (p.mode == 3) {
-    GF_LAUNCH(c, launch_conv_xy(c->dg, img[1], nullptr, g_fw, psf, st, store(1)));
+    GF_LAUNCH(c, launch_conv_xy(c->dg, img[1], g_fw, psf, st, store(1)));
     GF_TRY(project_all(psf, proj_t));
     GF_CK(cudaMemsetAsync(datos_v, 0, c->plan.ndata * sizeof(float), st));
   }
@@ -95,7 +95,7 @@ gf_status gf_recon::subiteration(int t, int s) {
   const int na = pl.sub_nang[s];
   const int64_t off = pl.sub_off[s];
   stage_begin(GF_STAGE_PSF);
-  GF_LAUNCH(c, launch_conv_xy(c->dg, img[t], nullptr, g_fw, psf, st, store(t)));
+  GF_LAUNCH(c, launch_conv_xy(c->dg, img[t], g_fw, psf, st, store(t)));
   stage_end();
   FpArgs a = c->fp_args(s, psf);
   if (p.mode == 3 && t == 1) {
@@ -118,7 +118,8 @@ gf_status gf_recon::subiteration(int t, int s) {
     GF_LAUNCH(c, launch_fp(a, c->fps, st));
     stage_end();
   }
-  BpArgs b = c->bp_args(s, corrcal, numer, denom, p.storage);
+  BpArgs b = c->bp_args(s, corrcal, ratio, nullptr, p.storage);
+  b.ratio = 1;
   // Triples data are mostly zero, and where a ratio of exactly 0 meets a
   // sentinel row the gap rule (GFIRST_GPU_Kernels.cu:157) turns on whether an
   // interpolation weight rounds to 0: the triples image follows the
@@ -128,8 +129,7 @@ gf_status gf_recon::subiteration(int t, int s) {
   GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
   stage_end();
   stage_begin(GF_STAGE_UPDATE);
-  GF_LAUNCH(c, launch_conv_xy(c->dg, numer, denom, g_bw, ctmp, st));
-  GF_LAUNCH(c, launch_zfilter_update(c->dg, ctmp, g5, img[t], st, store(t)));
+  GF_LAUNCH(c, launch_update(c->dg, ratio, g_bw, g5, img[t], st, store(t)));
   stage_end();
   if (t == 1 && s == pl.nsub - 1) {
     // GFIRST.cu:512-524: r=4, sigma3D=0.75, sigmaI=0.025, max_ref over the doubles image
@@ -185,34 +185,34 @@ gf_status fused_subiteration(gf_recon* const* G, int nfr, bool shared_mask) {
     f.fr[k].in = G[k]->img[0];
     f.fr[k].out = G[k]->psf;
   }
-  GF_LAUNCH(c, launch_conv_xy_frames(c->dg, f, nfr, false, r0->g_fw, st, r0->store(0)));
+  GF_LAUNCH(c, launch_conv_xy_frames(c->dg, f, nfr, r0->g_fw, st, r0->store(0)));
   FpArgs a = c->fp_args(s, nullptr);
   a.nfr = nfr;
   a.storage = r0->p.storage;
   for (int k = 0; k < nfr; k++)
     a.fr[k] = FpFrame{G[k]->psf, G[k]->dbg[0] + off, G[k]->cal + off, G[k]->corrcal, nullptr};
   GF_LAUNCH(c, launch_fp(a, c->fps, st));
-  BpArgs b = c->bp_args(s, r0->corrcal, r0->numer, r0->denom, r0->p.storage);
+  BpArgs b = c->bp_args(s, r0->corrcal, r0->ratio, nullptr, r0->p.storage);
+  b.ratio = 1;
   const int npair = (shared_mask && b.fast) ? nfr / 2 : 0;
   if (npair > 0) {
     // frames 2p and 2p + 1 share a warp per column; an odd last frame alone
     b.nfr = 2 * npair;
-    for (int k = 0; k < 2 * npair; k++) b.fr[k] = BpFrame{G[k]->corrcal, G[k]->numer, G[k]->denom};
+    for (int k = 0; k < 2 * npair; k++) b.fr[k] = BpFrame{G[k]->corrcal, G[k]->ratio, nullptr};
     GF_LAUNCH(c, launch_bp_pairs(b, c->bp_warps, st));
     if (nfr > 2 * npair) {
       b.nfr = 1;
-      b.fr[0] = BpFrame{G[nfr - 1]->corrcal, G[nfr - 1]->numer, G[nfr - 1]->denom};
+      b.fr[0] = BpFrame{G[nfr - 1]->corrcal, G[nfr - 1]->ratio, nullptr};
       GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
     }
   } else {
     b.nfr = nfr;
-    for (int k = 0; k < nfr; k++) b.fr[k] = BpFrame{G[k]->corrcal, G[k]->numer, G[k]->denom};
+    for (int k = 0; k < nfr; k++) b.fr[k] = BpFrame{G[k]->corrcal, G[k]->ratio, nullptr};
     GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
   }
   ImgFrames u{};
-  for (int k = 0; k < nfr; k++) u.fr[k] = ImgFrame{G[k]->numer, G[k]->denom, G[k]->ctmp, G[k]->img[0]};
-  GF_LAUNCH(c, launch_conv_xy_frames(c->dg, u, nfr, true, r0->g_bw, st));
-  GF_LAUNCH(c, launch_zfilter_update_frames(c->dg, u, nfr, r0->g5, st, r0->store(0)));
+  for (int k = 0; k < nfr; k++) u.fr[k] = ImgFrame{G[k]->ratio, nullptr, G[k]->img[0]};
+  GF_LAUNCH(c, launch_update_frames(c->dg, u, nfr, r0->g_bw, r0->g5, st, r0->store(0)));
   for (int k = 0; k < nfr; k++) G[k]->advance();
   return GF_OK;
 }
@@ -251,6 +251,7 @@ gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out)
   r->ctx = c;
   c->recons.push_back(r);
   r->p = *prm;
+  GF_CK(cudaEventCreateWithFlags(&r->ev_last, cudaEventDisableTiming));
   r->ntypes = prm->mode == 0 ? 0 : (prm->mode == 1 ? 1 : 2);
   const Plan& pl = c->plan;
   auto fail = [&](gf_status st) {
@@ -269,9 +270,7 @@ gf_status gf_recon_create(gf_ctx* c, const gf_recon_params* prm, gf_recon** out)
     if ((st = r->alloc((size_t)pl.nvoxp * (r->store(1) == GF_STORE_F32 ? 4 : 2), (void**)&r->img[1])) != GF_OK)
       return fail(st);
     ALLOC(r->psf, pl.nvoxp);
-    ALLOC(r->numer, pl.nvoxp);
-    ALLOC(r->denom, pl.nvoxp);
-    ALLOC(r->ctmp, pl.nvoxp);
+    ALLOC(r->ratio, pl.nvoxp);
     if ((st = r->alloc((size_t)pl.amax * pl.g.nrad * pl.PS * (prm->storage == GF_STORE_F32 ? 8 : 4), &r->corrcal)) != GF_OK)
       return fail(st);
     ALLOC(r->dbg[0], pl.all_elems());
@@ -306,6 +305,9 @@ void gf_recon_destroy(gf_recon* r) {
     cudaEventDestroy(e.a);
     cudaEventDestroy(e.b);
   }
+  if (r->ev_last) cudaEventDestroy(r->ev_last);
+  if (r->ev_staged) cudaEventDestroy(r->ev_staged);
+  if (r->ev_stage_free) cudaEventDestroy(r->ev_stage_free);
   delete r;
 }
 
@@ -339,6 +341,7 @@ static gf_status load_impl(gf_recon* r, const float* h_image, const float* h_dsi
     if ((s = ck(launch_file_to_zfast(c->dg, stage, img0, st), "layout")) != GF_OK) return done(s);
     if ((s = r->project_all(img0, r->proj_ref)) != GF_OK) return done(s);
     r->loaded = true;
+    r->mark();
     return done(GF_OK);
   }
   // STEP 1: projection of a unit cylinder -> proj_ref (GFIRST.cu:151-184).  It
@@ -350,11 +353,27 @@ static gf_status load_impl(gf_recon* r, const float* h_image, const float* h_dsi
     r->cyl_proj_ready = true;
   }
   // STEP 2: data (GFIRST.cu:207-260)
+  // The sinogram and normalization go to the device staging on the
+  // context's copy stream, so they can stream in while the context's
+  // compute stream still runs earlier work (another reconstruction's
+  // iterations); the layout kernels wait for them on the compute stream, and
+  // the next load's copies wait until those kernels have read the staging.
   float* s2 = stage;                      // 2*NDATA
   float* sn = stage + 2 * pl.ndata;       // NDATA
-  if ((s = ck(cudaMemcpyAsync(s2, h_dsino, 2 * pl.ndata * sizeof(float), cudaMemcpyHostToDevice, st), "upload sinogram")) != GF_OK) return done(s);
+  if (!r->ev_staged) {
+    if ((s = ck(cudaEventCreateWithFlags(&r->ev_staged, cudaEventDisableTiming), "event")) != GF_OK) return done(s);
+    if ((s = ck(cudaEventCreateWithFlags(&r->ev_stage_free, cudaEventDisableTiming), "event")) != GF_OK) return done(s);
+  }
+  cudaStream_t cs = c->copy_stream;
+  // first load: the staging was just allocated in the compute stream's order,
+  // so the copies wait for that point of it
+  if (!r->stage_used && (s = ck(cudaEventRecord(r->ev_stage_free, st), "record staging")) != GF_OK) return done(s);
+  if ((s = ck(cudaStreamWaitEvent(cs, r->ev_stage_free, 0), "wait staging")) != GF_OK) return done(s);
+  if ((s = ck(cudaMemcpyAsync(s2, h_dsino, 2 * pl.ndata * sizeof(float), cudaMemcpyHostToDevice, cs), "upload sinogram")) != GF_OK) return done(s);
+  if ((s = ck(cudaMemcpyAsync(sn, h_norm, pl.ndata * sizeof(float), cudaMemcpyHostToDevice, cs), "upload norm")) != GF_OK) return done(s);
+  if ((s = ck(cudaEventRecord(r->ev_staged, cs), "record staging")) != GF_OK) return done(s);
+  if ((s = ck(cudaStreamWaitEvent(st, r->ev_staged, 0), "wait upload")) != GF_OK) return done(s);
   if ((s = ck(launch_build_dbg(c->dg, c->d_rowmap, s2, r->dbg[0], st), "build data")) != GF_OK) return done(s);
-  if ((s = ck(cudaMemcpyAsync(sn, h_norm, pl.ndata * sizeof(float), cudaMemcpyHostToDevice, st), "upload norm")) != GF_OK) return done(s);
   if ((s = ck(launch_build_cal(c->dg, c->d_rowmap, r->proj_ref, sn, r->cal, st), "build mask")) != GF_OK) return done(s);
   if (mode >= 2) {
     if ((s = ck(cudaMemcpyAsync(s2, h_tsino, 2 * pl.ndata * sizeof(float), cudaMemcpyHostToDevice, st), "upload triples")) != GF_OK) return done(s);
@@ -396,8 +415,12 @@ static gf_status load_impl(gf_recon* r, const float* h_image, const float* h_dsi
     if ((s = ck(launch_vlor_count(c->dg, r->events, nevents, r->datos_v, st), "vlor count")) != GF_OK) return done(s);
     if ((s = ck(launch_blankt(c->dg, r->datos_v, s2, r->blankt, st), "blankt")) != GF_OK) return done(s);
   }
+  // the staging is free again once the compute stream has passed the layout kernels
+  if ((s = ck(cudaEventRecord(r->ev_stage_free, st), "record staging free")) != GF_OK) return done(s);
+  r->stage_used = true;
   if ((s = r->init_images()) != GF_OK) return done(s);
   r->loaded = true;
+  r->mark();
   return done(GF_OK);
 }
 
@@ -415,7 +438,9 @@ gf_status gf_recon_restart(gf_recon* r) {
   if (!r) return set_error(GF_ERR_ARG, "null reconstruction");
   if (!r->loaded) return set_error(GF_ERR_STATE, "gf_recon_load has not run");
   if (r->ntypes == 0) return GF_OK;
-  return r->init_images();
+  GF_TRY(r->init_images());
+  r->mark();
+  return GF_OK;
 }
 
 gf_status gf_recon_subiteration(gf_recon* r) {
@@ -424,6 +449,7 @@ gf_status gf_recon_subiteration(gf_recon* r) {
   if (r->ntypes == 0) return set_error(GF_ERR_STATE, "mode 0 has no iterations");
   GF_TRY(r->subiteration(r->cur_type, r->cur_sub));
   r->advance();
+  r->mark();
   return GF_OK;
 }
 
@@ -474,13 +500,18 @@ gf_status gf_recon_get_image(gf_recon* r, int32_t type, int32_t scaled, float* h
   if (type < 0 || type > 1 || !r->img[type]) return set_error(GF_ERR_ARG, "no such image");
   gf_ctx* c = r->ctx;
   const Plan& pl = c->plan;
+  // on the context's copy stream, after this reconstruction's own queued
+  // work only: work queued later for other reconstructions of the context
+  // (the next data set's iterations) is not waited for
+  cudaStream_t cs = c->copy_stream;
+  GF_CK(cudaStreamWaitEvent(cs, r->ev_last, 0));
   float* tmp = nullptr;
-  GF_CK(cudaMallocAsync(&tmp, pl.nvox * sizeof(float), c->stream));
+  GF_CK(cudaMallocAsync(&tmp, pl.nvox * sizeof(float), cs));
   const float scale = type == 0 ? r->p.scale_d : r->p.scale_t;
-  cudaError_t e = launch_zfast_to_file(c->dg, r->img[type], scale, scaled ? 1 : 0, tmp, c->stream, r->store(type));
-  if (e == cudaSuccess) e = cudaMemcpyAsync(h_out, tmp, pl.nvox * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
-  cudaFreeAsync(tmp, c->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaError_t e = launch_zfast_to_file(c->dg, r->img[type], scale, scaled ? 1 : 0, tmp, cs, r->store(type));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h_out, tmp, pl.nvox * sizeof(float), cudaMemcpyDeviceToHost, cs);
+  cudaFreeAsync(tmp, cs);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
   if (e != cudaSuccess) return cuda_error(e, "get image");
   return GF_OK;
 }

@@ -269,7 +269,7 @@ gf_status gf_recon_bytes(const gf_geometry* gg, int32_t nsub, const gf_recon_par
   if (p->mode == 0) {
     b += pl.nvox * 4;  // staging
   } else {
-    b += 5 * v;                                                                   // second image, psf, numer, denom, ctmp
+    b += 3 * v;                                                                   // second image, psf, ratio
     b += (int64_t)pl.amax * pl.g.nrad * pl.PS * (p->storage == GF_STORE_F32 ? 8 : 4);  // ratio sinogram
     b += all * 8 + all * 4;                                                       // data/background, mask
     b += 3 * d;                                                                   // staging

@@ -171,10 +171,10 @@ gf_status gf_vlor_split(gf_ctx* ctx, const int32_t* d_events, int64_t nevents, c
  * scratch exceeds it (image RES*RES*NZS padded to 32 slices, about 4.1 M
  * voxels) are rejected with GF_ERR_ARG.  Runs on the current device and on
  * `cuda_stream` (NULL: the legacy default stream).  The first call on a
- * device looks up the array's device address; make that call before any
- * stream capture.  The address is kept for the life of the process, so a
- * cudaDeviceReset of that device ends this entry point's use there.  All
- * calls share the array: calls whose work overlaps on the GPU race. */
+ * device looks up the array's device address and keeps it for the life of
+ * the process, so a cudaDeviceReset of that device ends this entry point's
+ * use there.  All calls share the array: calls whose work overlaps on the
+ * GPU race. */
 gf_status gf_forward_project_noalloc(const gf_geometry* g, int32_t nsubsets, int32_t subset, const float* d_image,
                                      float* d_proj, void* cuda_stream);
 
@@ -233,11 +233,13 @@ void gf_recon_destroy(gf_recon* r);
  * (GFIRST.cu:207-288).  Mode 0 takes h_image (NVOX floats) instead. */
 gf_status gf_recon_load(gf_recon* r, const float* h_image, const float* h_dsino, const float* h_tsino,
                         const float* h_norm, const int32_t* h_events, int64_t nevents);
-/* The same work queued on the context's stream without waiting for it (no
- * counterpart in the reference): the host buffers must stay untouched until
- * the stream has passed the load (gf_synchronize, or a call that returns
- * host results such as gf_recon_get_image).  With two reconstructions on two
- * contexts, the next data set loads while the current one iterates. */
+/* The same work queued without waiting for it (no counterpart in the
+ * reference): the host-to-device copies go on the context's copy stream, the
+ * data set-up that follows them on the context's stream.  The host buffers
+ * must stay untouched until the load has run (gf_synchronize, or a call that
+ * returns host results such as gf_recon_get_image).  With two
+ * reconstructions of one context, the next data set's copies overlap the
+ * current one's iterations. */
 gf_status gf_recon_load_async(gf_recon* r, const float* h_image, const float* h_dsino, const float* h_tsino,
                               const float* h_norm, const int32_t* h_events, int64_t nevents);
 /* Back to the initial images of GFIRST.cu:282-288 (and the initial triples
@@ -250,7 +252,10 @@ gf_status gf_recon_subiteration(gf_recon* r);
 /* Completed iterations and sub-iterations so far. */
 gf_status gf_recon_progress(const gf_recon* r, int32_t* iterations, int64_t* subiterations);
 /* Image of type 0 (doubles) or 1 (triples), file layout, NVOX floats.
- * scaled != 0 applies the output scaling and mask of GFIRST.cu:532-549. */
+ * scaled != 0 applies the output scaling and mask of GFIRST.cu:532-549.
+ * Waits for this reconstruction's queued work only: the read runs on the
+ * context's copy stream, so work queued since for other reconstructions of
+ * the context keeps running. */
 gf_status gf_recon_get_image(gf_recon* r, int32_t type, int32_t scaled, float* h_out);
 /* proj_ref.raw contents (GFIRST.cu:183-184), NDATA floats. */
 gf_status gf_recon_get_proj_ref(gf_recon* r, float* h_out);
