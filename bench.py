@@ -128,9 +128,9 @@ def peaks() -> tuple:
 def algorithmic_bytes(P: int, ndata: int, nvox: int) -> dict:
     """Compulsory HBM bytes per launch (one sub-iteration of 10 angles).
     FP: image read + per ray (data 4 + background 4 + mask 1 + ratio out 4).
-    BP: per bin (ratio 4 + mask 1) + NUMER and DENOM written."""
+    BP: per bin (ratio 4 + mask 1) + the update ratio NUMER/DENOM written."""
     bins_sub = ndata // NSUB
-    return {"fp": nvox * 4 + bins_sub * 13, "bp": bins_sub * 5 + nvox * 8}
+    return {"fp": nvox * 4 + bins_sub * 13, "bp": bins_sub * 5 + nvox * 4}
 
 
 def committed_traffic() -> dict:
@@ -488,22 +488,31 @@ def run_gpu(args) -> int:
         phases = {k: statistics.median(v) for k, v in phases.items()}
         barrier()
         t0 = time.perf_counter()
+        seq_ms = []
         for k in range(args.e2e_steps):  # one reconstruction at a time
+            ts = time.perf_counter()
             issue(0, wait=True)
             read(0)
+            seq_ms.append(1000 * (time.perf_counter() - ts))
         dt_seq = max_over_ranks(time.perf_counter() - t0, dist)
         barrier()
         t0 = time.perf_counter()
+        step_ms = []  # host clock from one image's read-back to the next
+        ts = t0
         issue(0)
         for k in range(args.e2e_steps):
             if k + 1 < args.e2e_steps:
                 issue(k + 1)
             read(k)
+            t1 = time.perf_counter()
+            step_ms.append(1000 * (t1 - ts))
+            ts = t1
         torch.cuda.synchronize()
         dt = max_over_ranks(time.perf_counter() - t0, dist)
         e2e = {"value": whole_job_rate(world, NSUB * NITER * args.e2e_steps, dt), "unit": UNIT,
                "h2d_bytes_per_step": (n2 + ndata) * 4, "d2h_bytes_per_step": nvox * 4,
                "steps": args.e2e_steps, "ms_per_step": 1000.0 * dt / args.e2e_steps,
+               "step_ms": [round(x, 2) for x in step_ms],
                "path": "per step: gf_recon_load_async(pinned host sinogram+normalization) + gf_recon_iterate(2) + "
                        "gf_recon_get_image(scaled); two reconstructions of one context alternate, the next "
                        "step's upload (copy stream) and iterations queued before this step's image is read "
@@ -511,6 +520,7 @@ def run_gpu(args) -> int:
                "sequential_phases": phases,
                "sequential": {"value": whole_job_rate(world, NSUB * NITER * args.e2e_steps, dt_seq),
                               "ms_per_step": 1000.0 * dt_seq / args.e2e_steps,
+                              "step_ms": [round(x, 2) for x in seq_ms],
                               "path": "gf_recon_load + gf_recon_iterate(2) + gf_recon_get_image, one "
                                       "reconstruction, each step after the previous one"}}
         for rr in recs:
@@ -1249,7 +1259,7 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference", "reference-shim"])
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=12)
     ap.add_argument("--fp64-steps", type=int, default=4, help="sub-iterations of the FP64 oracle for the "
                     "headline's accuracy field (0: FP32 oracle only)")

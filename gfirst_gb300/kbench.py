@@ -1,16 +1,19 @@
 """Kernel micro-benchmark: time one projector stage on a named geometry.
 
     python -m gfirst_gb300.kbench --op bp|fp|subiter [--geometry preclinical] [--subsets 16] [--reps 5]
-                                  [--storage f32|f16|bf16] [--tune] [--bp-form view|voxel]
+                                  [--storage f32|f16|bf16] [--tune] [--bp-form view|voxel] [--pairs]
 
 Runs a mode-1 reconstruction's stages on synthetic data and reports the
-device time per launch from the library's own stage events.  Small enough to
-run under a profiler (one context, one reconstruction, a few launches).
+device time per launch from the library's own stage events.  With --pairs,
+two frames of one normalization run as a fused group instead (the paired
+back projector), timed per frame and iteration on the host clock.  Small
+enough to run under a profiler (one context, a few launches).
 """
 from __future__ import annotations
 
 import argparse
 import json
+import time
 
 import numpy as np
 
@@ -20,7 +23,7 @@ GEOMS = {"preclinical": gf.Geometry.preclinical, "reference": gf.Geometry.refere
 
 
 def run(op: str, geometry: str, nsub: int, reps: int, storage: str = "f32", tune: bool = False,
-        bp_form: str = "view") -> dict:
+        bp_form: str = "view", pairs: bool = False) -> dict:
     g = GEOMS[geometry]()
     ctx = gf.Context(g, nsub=nsub)
     ctx.set_bp_form(bp_form)
@@ -31,6 +34,24 @@ def run(op: str, geometry: str, nsub: int, reps: int, storage: str = "f32", tune
     norm = rs.uniform(0.85, 1.15, ndata).astype(np.float32)
     r = gf.Recon(ctx, 1, niter=1, storage=storage)
     r.load(dsino=dsino, norm=norm)
+    if pairs:
+        r2 = gf.Recon(ctx, 1, niter=1, storage=storage)
+        r2.load(dsino=np.roll(dsino, 17), norm=norm)
+        b = gf.Batch([r, r2])
+        b.set_fused(True, pairs=True)
+        b.iterate(1, graph=False)  # warm-up
+        b.sync()
+        t0 = time.perf_counter()
+        b.iterate(reps, graph=False)
+        b.sync()
+        dt = time.perf_counter() - t0
+        out = {"geometry": geometry, "subsets": nsub, "reps": reps, "storage": storage, "tuned": tuned,
+               "bp_form": bp_form, "groups": b.groups(), "ms_per_frame_iteration": 1000 * dt / (2 * reps)}
+        b.close()
+        r2.close()
+        r.close()
+        ctx.close()
+        return out
     r.subiteration()  # warm-up
     r.profile(True)
     for _ in range(reps):
@@ -55,8 +76,9 @@ def main() -> None:
     ap.add_argument("--storage", default="f32", choices=["f32", "f16", "bf16"])
     ap.add_argument("--tune", action="store_true")
     ap.add_argument("--bp-form", default="view", choices=["voxel", "view"])
+    ap.add_argument("--pairs", action="store_true")
     a = ap.parse_args()
-    print(json.dumps(run(a.op, a.geometry, a.subsets, a.reps, a.storage, a.tune, a.bp_form)))
+    print(json.dumps(run(a.op, a.geometry, a.subsets, a.reps, a.storage, a.tune, a.bp_form, a.pairs)))
 
 
 if __name__ == "__main__":

@@ -752,6 +752,36 @@ def test_async_load_on_two_streams_matches_sync_load(gf):
         assert np.array_equal(rb.image(0), ref[1])
 
 
+def test_pipelined_loads_on_one_context_match_sync_loads(gf):
+    """Two reconstructions of one context, pipelined as a host streaming data
+    sets would: the next set's load (its copies on the context's copy stream)
+    and iterations are queued before the current image is read (on the copy
+    stream, after that reconstruction's own work only).  Every image equals
+    the one a plain load and read gives."""
+    d = parsed("tinyb")
+    g = gf.Geometry(*case("tinyb"))
+    sets = [np.roll(d["dsino"], 5 * k) for k in range(5)]
+    c = gf.Context(g, nsub=2)
+    r = gf.Recon(c, 1, niter=2)
+    ref = []
+    for ds in sets:
+        r.load(dsino=ds, norm=d["norm"])
+        r.iterate(2)
+        ref.append(r.image(0))
+    ctx = gf.Context(g, nsub=2)
+    recs = [gf.Recon(ctx, 1, niter=2), gf.Recon(ctx, 1, niter=2)]
+
+    def issue(k):
+        recs[k % 2].load(dsino=sets[k], norm=d["norm"], wait=False)
+        recs[k % 2].iterate(2)
+
+    issue(0)
+    for k in range(len(sets)):
+        if k + 1 < len(sets):
+            issue(k + 1)
+        assert np.array_equal(recs[k % 2].image(0), ref[k]), k
+
+
 def test_reload_keeps_geometry_projection_and_results(gf):
     """A second load into the same reconstruction reuses the cylinder projection
     and gives the same images as a fresh reconstruction of the new data."""
