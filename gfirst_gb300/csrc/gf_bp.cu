@@ -7,7 +7,8 @@
 //
 // GB300 design.  One warp owns one image column (x, y); lane l holds voxels
 // z = l, l+32, ... and their (NUMER, DENOM) pairs in registers for the whole
-// subset, so the volumes are written once per sub-iteration.  For a column
+// subset, so the volumes (or, in a reconstruction, their update ratio) are
+// written once per sub-iteration.  For a column
 // and an angle the radial coordinate is fixed, so per (segment, angle) view:
 //  (1) the warp interpolates every plane row of the view radially once
 //      (lanes along rows: coalesced 8-byte (corr, calib) loads from the

@@ -11,8 +11,10 @@
  *  - `d_` pointers are device memory, `h_` pointers host memory;
  *  - device arrays use the reference's layouts: images [NZS][RES][RES]
  *    (x fastest), sinograms [P][NANG][NRAD] (radial fastest), P = planes;
- *  - work is queued on the context's stream (gf_set_stream); calls that take
- *    host buffers return after their results are in host memory;
+ *  - work is queued on the context's stream (gf_set_stream); a
+ *    reconstruction's host-to-device loads and image read-backs run on the
+ *    context's own copy stream, ordered against that stream by events; calls
+ *    that take host buffers return after their results are in host memory;
  *  - a context is used by one host thread at a time.
  */
 #ifndef GFIRST_H
