@@ -284,6 +284,24 @@ def test_psf_and_update_bit_exact(gf, name):
     assert np.array_equal(dimg.download(), o.update(img, numer, denom, 1.5))
 
 
+# The update kernel works on chunks of 28 output slices (27 where slice NZS-1
+# would start a chunk: 29, 57, 85, ..., 253) with two halo slices either side
+# and takes the edge-slice copies from its neighbour lanes.
+@pytest.mark.parametrize("nzs", [5, 6, 29, 30, 31, 57, 58, 85, 113, 141, 159, 169, 253, 256])
+def test_update_across_axial_sizes_bit_exact(gf, nzs):
+    geo = (12, nzs, 16, 12, 1, 1, 1.6, 20.7219750, 12.5)
+    o = gfo.Oracle(geo)
+    ctx = gf.Context(gf.Geometry(*geo))
+    rs = np.random.RandomState(nzs)
+    img = rs.uniform(0.5, 2, o.nvox).astype(np.float32)
+    numer = rs.uniform(0, 4, o.nvox).astype(np.float32)
+    denom = rs.uniform(0, 4, o.nvox).astype(np.float32)
+    denom[rs.uniform(size=o.nvox) < 0.05] = 0.0005
+    dimg = ctx.put(img)
+    ctx.image_update(dimg, ctx.put(numer), ctx.put(denom), 1.5)
+    assert np.array_equal(dimg.download(), o.update(img, numer, denom, 1.5))
+
+
 def test_bilateral_matches_oracle(gf):
     geo = case("tinyb")
     o = gfo.Oracle(geo)
