@@ -513,6 +513,7 @@ def run_gpu(args) -> int:
                "h2d_bytes_per_step": (n2 + ndata) * 4, "d2h_bytes_per_step": nvox * 4,
                "steps": args.e2e_steps, "ms_per_step": 1000.0 * dt / args.e2e_steps,
                "step_ms": [round(x, 2) for x in step_ms],
+               "median_step_ms": round(statistics.median(step_ms), 2),
                "path": "per step: gf_recon_load_async(pinned host sinogram+normalization) + gf_recon_iterate(2) + "
                        "gf_recon_get_image(scaled); two reconstructions of one context alternate, the next "
                        "step's upload (copy stream) and iterations queued before this step's image is read "
@@ -647,9 +648,11 @@ def run_frames(args) -> int:
     with the default tile shapes.  Batched: FP16 storage of the ratio sinogram,
     autotuned tile shapes, every frame's iteration replayed from one CUDA graph
     (frames run as parallel branches); batched_f32 the same in FP32 storage.
-    Fused (and fused_f32): the same graph with the frames of equal subset count
-    fused into groups that run every stage as one launch, the back projection
-    two frames per warp (the frames share the scanner's normalization);
+    Fused (and fused_f32): the same graph with the frames fused into groups of
+    up to 16 whatever their subset counts (one tuned tile-shape set for every
+    frame), each step of a group one launch per stage over the frames that
+    have that subset, the back projection two frames per warp for frames of
+    one subset count (the frames share the scanner's normalization);
     fused_launch_only: the groups with one frame per warp (gf_batch_set_fused).
     Data resident in HBM in every arm.  The first and last frames of every arm
     are compared with the FP64 oracle (--fp64-oracle 0 skips that)."""
@@ -678,17 +681,21 @@ def run_frames(args) -> int:
     del pb, po, gains
     torch.cuda.empty_cache()
 
-    def build(storage: str, tune: bool):
+    def build(storage: str, tune: bool, one_shape: bool = False):
         ctxs, recs, tuned = [], [], []
-        shapes = {}  # tuned once per subset count, then set on the other frames' contexts
+        # tuned once per subset count (one_shape: once for all frames, so that
+        # frames of every count can share a fused launch), then set on the
+        # other frames' contexts
+        shapes = {}
         for k in range(nf):
             c = gf.Context(g, nsub=int(nsubs[k]))
-            if tune and int(nsubs[k]) not in shapes:
-                shapes[int(nsubs[k])] = c.tune()
+            key = 0 if one_shape else int(nsubs[k])
+            if tune and key not in shapes:
+                shapes[key] = c.tune()
             elif tune:
-                t = shapes[int(nsubs[k])]
+                t = shapes[key]
                 c.set_tile_shapes(t["fp_run"], t["fp_chunk"], t["bp_warps"])
-            tuned.append(shapes.get(int(nsubs[k])) if tune else None)
+            tuned.append(shapes.get(key) if tune else None)
             r = gf.Recon(c, 1, niter=niter, storage=storage)
             r.load(dsino=data[k][0], norm=data[k][1])
             r._keep = None
@@ -704,7 +711,7 @@ def run_frames(args) -> int:
     arms = {"plain": ("f32", False, 0), "batched_f32": ("f32", True, 0), "batched": ("f16", True, 0),
             "fused_launch_only": ("f16", True, 2), "fused_f32": ("f32", True, 1), "fused": ("f16", True, 1)}
     for arm, (storage, batched, fused) in arms.items():
-        ctxs, recs, tuned = build(storage, batched)
+        ctxs, recs, tuned = build(storage, batched, one_shape=fused > 0)
         batch = gf.Batch(recs) if batched else None
         if fused:
             batch.set_fused(True, pairs=fused == 1)

@@ -362,9 +362,10 @@ class Batch:
         self.h = h
 
     def set_fused(self, fused: bool = True, pairs: bool = True) -> None:
-        """Fused groups: frames that match run each stage as one launch; with
-        pairs, frames of equal normalization back-project two per warp
-        (gf_batch_set_fused 1, else 2; fused=False: 0)."""
+        """Fused groups: frames that match (any subset counts) run each stage
+        as one launch; with pairs, frames of one subset count and equal
+        normalization back-project two per warp (gf_batch_set_fused 1, else 2;
+        fused=False: 0)."""
         _ck(lib().gf_batch_set_fused(self.h, 0 if not fused else (1 if pairs else 2)))
 
     def groups(self) -> tuple:

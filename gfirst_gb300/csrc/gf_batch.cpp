@@ -2,13 +2,13 @@
 //
 // Each frame is a loaded gf_recon with its own resident data, subset count
 // and stream.  The frames are split into units: with fusing on
-// (gf_batch_set_fused), mode-1 frames that share geometry, subset count,
-// storage, filters and tile shapes form fused groups of up to kMaxFrames,
-// whose sub-iterations run every stage as one launch over the group
-// (fused_subiteration); every other frame is a unit of its own.  In a group
-// whose frames' normalization masks are equal (the frames of one scanner
-// and normalization), the back projection runs two frames per warp, sharing
-// the per-view geometry and the mask rows.
+// (gf_batch_set_fused), mode-1 frames that share geometry, storage, filters
+// and tile shapes form fused groups of up to kMaxFrames, whatever their
+// subset counts, whose sub-iterations run every stage as one launch over the
+// frames that have that subset (fused_subiteration); every other frame is a
+// unit of its own.  Frames of a group with the same subset count and equal
+// normalization masks (the frames of one scanner and normalization)
+// back-project two per warp, sharing the per-view geometry and the mask rows.
 //
 // One iteration of every unit is captured once: a fork event on the batch's
 // origin stream, each unit's kernels on the stream of its first frame (a
@@ -34,7 +34,9 @@ struct gf_batch {
   int device = 0;
   int fused = 0;  // gf_batch_set_fused: 0 off, 1 groups (paired back projection where masks match), 2 groups
   std::vector<std::vector<int>> units;  // frame indices: a fused group, or one frame
-  std::vector<bool> shared_mask;        // per unit: every frame's normalization mask equals the first's
+  // per unit and member: its pairing class (the first member with the same
+  // subset count and an equal normalization mask), or -1 (back-projected alone)
+  std::vector<std::vector<int>> cls;
   int* d_flag = nullptr;                // device flag of the mask comparison
   cudaStream_t origin = nullptr;
   cudaEvent_t fork = nullptr;
@@ -78,43 +80,66 @@ static void make_units(gf_batch* b) {
   }
 }
 
-// Which fused groups may back-project two frames per warp: those whose
-// frames' static normalization masks (every subset) are equal to the first
-// frame's, bit for bit, compared on the device after the frames' queued work
-// (their loads) has finished.
+// Which frames of a fused group may back-project two per warp: those with
+// the same subset count whose static normalization masks (every subset, in
+// that count's layout) are equal bit for bit, compared on the device after
+// the frames' queued work (their loads) has finished.
 static gf_status check_masks(gf_batch* b) {
-  b->shared_mask.assign(b->units.size(), false);
-  if (b->fused != 1) return GF_OK;
+  b->cls.assign(b->units.size(), {});
   for (size_t k = 0; k < b->units.size(); k++) {
     const auto& u = b->units[k];
-    if (u.size() < 2) continue;
-    const gf_recon* r0 = b->frames[u[0]];
-    if (r0->ctx->bp_form != GF_BP_PER_VIEW) continue;
-    bool same = true;
-    for (size_t j = 1; j < u.size() && same; j++) {
+    b->cls[k].assign(u.size(), -1);
+    if (b->fused != 1 || u.size() < 2) continue;
+    if (b->frames[u[0]]->ctx->bp_form != GF_BP_PER_VIEW) continue;
+    for (size_t j = 0; j < u.size(); j++) {
       const gf_recon* r = b->frames[u[j]];
-      GF_CK(cudaStreamSynchronize(r0->ctx->stream));
-      GF_CK(cudaStreamSynchronize(r->ctx->stream));
-      if (r->cal == r0->cal) continue;
-      GF_CK(launch_differs(r0->cal, r->cal, (size_t)r0->ctx->plan.all_elems(), b->d_flag, b->origin));
-      int flag = 1;
-      GF_CK(cudaMemcpyAsync(&flag, b->d_flag, sizeof(int), cudaMemcpyDeviceToHost, b->origin));
-      GF_CK(cudaStreamSynchronize(b->origin));
-      same = flag == 0;
+      b->cls[k][j] = (int)j;  // a class of its own unless an earlier leader matches
+      for (size_t i = 0; i < j; i++) {
+        if (b->cls[k][i] != (int)i) continue;  // not a class leader
+        const gf_recon* l = b->frames[u[i]];
+        if (l->ctx->plan.nsub != r->ctx->plan.nsub) continue;
+        bool same = l->cal == r->cal;
+        if (!same) {
+          GF_CK(cudaStreamSynchronize(l->ctx->stream));
+          GF_CK(cudaStreamSynchronize(r->ctx->stream));
+          GF_CK(launch_differs(l->cal, r->cal, (size_t)l->ctx->plan.all_elems(), b->d_flag, b->origin));
+          int flag = 1;
+          GF_CK(cudaMemcpyAsync(&flag, b->d_flag, sizeof(int), cudaMemcpyDeviceToHost, b->origin));
+          GF_CK(cudaStreamSynchronize(b->origin));
+          same = flag == 0;
+        }
+        if (same) {
+          b->cls[k][j] = (int)i;
+          break;
+        }
+      }
     }
-    b->shared_mask[k] = same;
   }
   return GF_OK;
 }
 
-// One iteration of one unit on its first frame's stream.
+// One iteration of one unit on its first frame's stream.  A fused group's
+// frames may differ in subset count: step s runs the frames that have a
+// subset s, each at its own subset s, so every frame visits its subsets in
+// order as it would alone.
 static gf_status unit_iteration(gf_batch* b, size_t k) {
   const std::vector<int>& u = b->units[k];
   if (u.size() == 1) return gf_recon_iterate(b->frames[u[0]], 1);
-  std::vector<gf_recon*> G;
-  for (int i : u) G.push_back(b->frames[i]);
-  for (int s = 0; s < G[0]->ctx->plan.nsub; s++)
-    GF_TRY(fused_subiteration(G.data(), (int)G.size(), b->shared_mask[k]));
+  // the group's work stays on its first member's stream in every step
+  cudaStream_t st = b->frames[u[0]]->ctx->stream;
+  int smax = 0;
+  for (int i : u) smax = std::max(smax, b->frames[i]->ctx->plan.nsub);
+  for (int s = 0; s < smax; s++) {
+    std::vector<gf_recon*> G;
+    std::vector<int> C;
+    for (size_t j = 0; j < u.size(); j++) {
+      gf_recon* r = b->frames[u[j]];
+      if (r->ctx->plan.nsub <= s) continue;
+      G.push_back(r);
+      C.push_back(b->cls[k][j]);
+    }
+    GF_TRY(fused_subiteration(G.data(), (int)G.size(), C.data(), st));
+  }
   return GF_OK;
 }
 
@@ -182,7 +207,10 @@ gf_status gf_batch_groups(gf_batch* b, int32_t* ngroups, int32_t* largest, int32
   for (size_t k = 0; k < b->units.size(); k++) {
     n++;
     big = std::max(big, (int)b->units[k].size());
-    if (b->shared_mask[k]) pairs += (int)b->units[k].size() / 2;
+    // pairs of the first step, where every member takes part
+    const std::vector<int>& c = b->cls[k];
+    for (size_t j = 0; j < c.size(); j++)
+      if (c[j] == (int)j) pairs += (int)std::count(c.begin(), c.end(), (int)j) / 2;
   }
   if (ngroups) *ngroups = n;
   if (largest) *largest = big;

@@ -44,8 +44,9 @@ __device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v,
 // 1 where DENOM < 0.001.
 __device__ __forceinline__ float update_ratio(float n, float d) { return d < 0.001f ? 1.0f : __fdiv_rn(n, d); }
 
-// Angle index of the l-th angle of subset s.
-__device__ __forceinline__ int subset_angle(const DevGeom& g, int s, int l) { return s + l * g.nsub; }
+// Angle index of the l-th angle of subset s of nsub.
+__device__ __forceinline__ int subset_angle(int s, int nsub, int l) { return s + l * nsub; }
+__device__ __forceinline__ int subset_angle(const DevGeom& g, int s, int l) { return subset_angle(s, g.nsub, l); }
 #endif
 
 }  // namespace gf

@@ -35,8 +35,9 @@ __global__ void __launch_bounds__(512) fp_kernel(const FpArgs a) {
   const DevGeom& g = a.g;
   const FpFrame& F = a.fr[blockIdx.z];
   const int ird = blockIdx.x, tl = blockIdx.y;
+  if (tl >= F.na) return;  // a frame with fewer angles in its subset than the launch's largest
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int theta = subset_angle(g, a.subset, tl);
+  const int theta = subset_angle(F.subset, F.nsub, tl);
   const float2 sc = g.trig[theta];
   const float sn = sc.x, cs = sc.y;
   // GFIRST_GPU_Kernels.cu:79-87 (fac = RES/NPT = 1 makes dx = sin, dy = -cos exactly)
@@ -146,7 +147,8 @@ static cudaError_t launch_fp_t(const FpArgs& a, const FpSchedule& s, cudaStream_
   size_t smem = s.smem_bytes();
   cudaError_t e = allow_max_smem(k);
   if (e != cudaSuccess) return e;
-  int na = (a.g.nang - a.subset + a.g.nsub - 1) / a.g.nsub;
+  int na = 0;
+  for (int f = 0; f < (a.nfr > 1 ? a.nfr : 1); f++) na = a.fr[f].na > na ? a.fr[f].na : na;
   dim3 grid(a.g.nrad, na, a.nfr > 1 ? a.nfr : 1);
   k<<<grid, s.nthreads, smem, st>>>(a);
   return cudaGetLastError();
@@ -172,6 +174,10 @@ cudaError_t launch_fp(const FpArgs& a, const FpSchedule& s, cudaStream_t st) {
     if (!F.img || (!F.corrcal && !F.proj_full)) return cudaErrorInvalidValue;
     if (!F.corrcal != !a.fr[0].corrcal || !F.proj_full != !a.fr[0].proj_full) return cudaErrorInvalidValue;
     if (F.corrcal && (!F.dbg || !F.cal)) return cudaErrorInvalidValue;
+    // the subset's angles: subset + l*nsub for l < na, all inside [0, nang)
+    if (F.nsub < 1 || F.subset < 0 || F.subset >= F.nsub || F.na < 1 ||
+        F.na != (a.g.nang - F.subset + F.nsub - 1) / F.nsub)
+      return cudaErrorInvalidValue;
   }
   if (a.fr[0].corrcal && a.fr[0].proj_full && a.storage != 0) return cudaErrorInvalidValue;
   switch (s.R) {

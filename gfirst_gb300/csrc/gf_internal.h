@@ -157,15 +157,17 @@ struct gf_recon {
 };
 
 namespace gf {
-// Frames a fused group may hold together: mode 1, one device, the same
-// geometry and subset count, storage, filters, back-projector form and tile
-// shapes, so one launch per stage serves them all.
+// Whether two loaded frames can share a fused launch: mode 1, one device and
+// geometry, the same storage, filters, back-projector form and tile shapes
+// (the subset counts may differ), so one launch per stage serves them all.
 bool fusable(const gf_recon* a, const gf_recon* b);
-// One sub-iteration of every frame of a fused group (all at the same
-// subset): the forward PSF, projection + ratio, back projection and update
-// are one launch each over the nfr <= kMaxFrames frames, on the first
-// frame's stream and with its tables.  Advances every frame's cursor.
-// With shared_mask (every frame's normalization mask equal to the first's,
-// per-view back projector) the back projection runs two frames per warp.
-gf_status fused_subiteration(gf_recon* const* G, int nfr, bool shared_mask = false);
+// One sub-iteration of every frame of a fused group, all at the same subset
+// index s, each at subset s of its own subset count: the forward PSF,
+// projection + ratio, back projection and update are one launch each over
+// the nfr <= kMaxFrames frames, on stream st (the group's: its first
+// member's, which need not take part in every step) with the first
+// frame's tables.  Advances every frame's cursor.  cls: frames with the same
+// class >= 0 (same subset count and normalization mask; per-view back
+// projector) back-project two per warp.
+gf_status fused_subiteration(gf_recon* const* G, int nfr, const int* cls, cudaStream_t st);
 }  // namespace gf

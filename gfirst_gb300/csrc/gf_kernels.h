@@ -18,10 +18,12 @@ template <> struct PairT<2> { using type = __nv_bfloat162; };
 struct Taps9 { float c[9]; };
 struct Taps5 { float c[5]; };
 
-// One launch may serve several frames of one geometry and subset (a fused
-// group of a batch): every per-frame buffer sits in a table of kMaxFrames
-// entries passed by value, the launch has one grid slice per frame, and a
-// block takes its frame's entry.  A single-frame launch fills entry 0.
+// One launch may serve several frames of one geometry (a fused group of a
+// batch): every per-frame buffer sits in a table of kMaxFrames entries passed
+// by value, the launch has one grid slice per frame, and a block takes its
+// frame's entry.  Frames may differ in subset count: each entry names its
+// frame's subset (angles subset + l*nsub, l < na).  A single-frame launch
+// fills entry 0.
 constexpr int kMaxFrames = 16;
 
 // ---- forward projector (gf_fp.cu) ----
@@ -31,10 +33,10 @@ struct FpFrame {
   const float* cal;        // subset layout normalization mask; with corrcal
   void* corrcal;           // subset layout (corr, calib) pairs output, or null
   float* proj_full;        // file-layout projection output, or null
+  int subset, nsub, na;    // the frame's subset, its subset count and the subset's angles
 };
 struct FpArgs {
-  DevGeom g;
-  int subset;
+  DevGeom g;               // g.nsub unused: each frame names its own
   const int4* runs;        // FpSchedule::runs as (seg, p0, n, pad)
   int nruns, padl, cw, lc;
   int storage;             // corrcal pair type: 0 float2, 1 __half2, 2 __nv_bfloat162
@@ -48,10 +50,11 @@ struct BpFrame {
   const void* corrcal;     // subset layout (corr, calib) pairs
   float* numer;            // z-fast
   float* denom;            // z-fast
+  int subset, nsub, na;    // as FpFrame
 };
 struct BpArgs {
-  DevGeom g;
-  int subset, na;          // na: angles in this subset
+  DevGeom g;               // g.nsub unused: each frame names its own
+  int na;                  // the most angles of any frame's subset (shared-memory tables)
   int nfr;                 // frames in this launch (grid y); 0 is taken as 1
   BpFrame fr[kMaxFrames];
   int storage;             // corrcal pair type, as FpArgs::storage

@@ -100,9 +100,11 @@ extern "C" gf_status gf_forward_project_noalloc(const gf_geometry* gg, int32_t n
   GF_CK(launch_file_to_zfast(dg, d_image, img, st));
   FpArgs a{};
   a.g = dg;
-  a.subset = subset;
   a.nfr = 1;
   a.fr[0].img = img;
+  a.fr[0].subset = subset;
+  a.fr[0].nsub = plan.nsub;
+  a.fr[0].na = plan.sub_nang[subset];
   a.runs = druns;
   a.nruns = (int)fps.runs.size();
   a.padl = fps.padl;

@@ -163,51 +163,73 @@ bool fusable(const gf_recon* a, const gf_recon* b) {
   const bool same_geom = g.res == h.res && g.nzs == h.nzs && g.nrad == h.nrad && g.nang == h.nang &&
                          g.span == h.span && g.nseg == h.nseg && g.pitch == h.pitch && g.diam == h.diam &&
                          g.fov == h.fov;
+  // the subset counts may differ: each frame's launch entry names its subset
   return a->p.mode == 1 && b->p.mode == 1 && a->loaded && b->loaded && x->device == y->device && same_geom &&
-         x->plan.nsub == y->plan.nsub && a->p.storage == b->p.storage &&
-         a->p.image_storage == b->p.image_storage && a->p.psf_fw == b->p.psf_fw && a->p.psf_bw == b->p.psf_bw &&
-         x->bp_form == y->bp_form && x->bp_warps == y->bp_warps && x->fps.R == y->fps.R && x->fps.lc == y->fps.lc;
+         a->p.storage == b->p.storage && a->p.image_storage == b->p.image_storage && a->p.psf_fw == b->p.psf_fw &&
+         a->p.psf_bw == b->p.psf_bw && x->bp_form == y->bp_form && x->bp_warps == y->bp_warps &&
+         x->fps.R == y->fps.R && x->fps.lc == y->fps.lc;
 }
 
-gf_status fused_subiteration(gf_recon* const* G, int nfr, bool shared_mask) {
+gf_status fused_subiteration(gf_recon* const* G, int nfr, const int* cls, cudaStream_t st) {
   if (nfr < 1 || nfr > kMaxFrames) return set_error(GF_ERR_ARG, "fused group size out of range");
   gf_recon* r0 = G[0];
   gf_ctx* c = r0->ctx;
-  const Plan& pl = c->plan;
-  cudaStream_t st = c->stream;
   const int s = r0->cur_sub;
   for (int k = 1; k < nfr; k++)
     if (G[k]->cur_sub != s || G[k]->cur_type != 0 || !fusable(r0, G[k]))
       return set_error(GF_ERR_STATE, "frames of a fused group must match and stand at the same subset");
-  const int64_t off = pl.sub_off[s];
   ImgFrames f{};
   for (int k = 0; k < nfr; k++) {
     f.fr[k].in = G[k]->img[0];
     f.fr[k].out = G[k]->psf;
   }
   GF_LAUNCH(c, launch_conv_xy_frames(c->dg, f, nfr, r0->g_fw, st, r0->store(0)));
+  // every frame at subset s of its own subset count: its own angles and its
+  // own offset into the subset-ordered data
   FpArgs a = c->fp_args(s, nullptr);
   a.nfr = nfr;
   a.storage = r0->p.storage;
-  for (int k = 0; k < nfr; k++)
-    a.fr[k] = FpFrame{G[k]->psf, G[k]->dbg[0] + off, G[k]->cal + off, G[k]->corrcal, nullptr};
+  std::vector<BpFrame> bf(nfr);
+  int na_max = 0;
+  for (int k = 0; k < nfr; k++) {
+    const Plan& pk = G[k]->ctx->plan;
+    const int64_t off = pk.sub_off[s];
+    const int na = pk.sub_nang[s];
+    a.fr[k] = FpFrame{G[k]->psf, G[k]->dbg[0] + off, G[k]->cal + off, G[k]->corrcal, nullptr, s, pk.nsub, na};
+    bf[k] = BpFrame{G[k]->corrcal, G[k]->ratio, nullptr, s, pk.nsub, na};
+    na_max = std::max(na_max, na);
+  }
   GF_LAUNCH(c, launch_fp(a, c->fps, st));
   BpArgs b = c->bp_args(s, r0->corrcal, r0->ratio, nullptr, r0->p.storage);
   b.ratio = 1;
-  const int npair = (shared_mask && b.fast) ? nfr / 2 : 0;
-  if (npair > 0) {
-    // frames 2p and 2p + 1 share a warp per column; an odd last frame alone
-    b.nfr = 2 * npair;
-    for (int k = 0; k < 2 * npair; k++) b.fr[k] = BpFrame{G[k]->corrcal, G[k]->ratio, nullptr};
-    GF_LAUNCH(c, launch_bp_pairs(b, c->bp_warps, st));
-    if (nfr > 2 * npair) {
-      b.nfr = 1;
-      b.fr[0] = BpFrame{G[nfr - 1]->corrcal, G[nfr - 1]->ratio, nullptr};
-      GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
+  b.na = na_max;
+  // frames of one class (same subset count and normalization mask) share a
+  // warp per column two by two; the rest go alone
+  std::vector<int> pairs, singles;
+  std::vector<bool> used(nfr, false);
+  for (int k = 0; k < nfr; k++) {
+    if (used[k]) continue;
+    used[k] = true;
+    int j = -1;
+    if (b.fast && cls && cls[k] >= 0)
+      for (int m = k + 1; m < nfr && j < 0; m++)
+        if (!used[m] && cls[m] == cls[k]) j = m;
+    if (j >= 0) {
+      used[j] = true;
+      pairs.push_back(k);
+      pairs.push_back(j);
+    } else {
+      singles.push_back(k);
     }
-  } else {
-    b.nfr = nfr;
-    for (int k = 0; k < nfr; k++) b.fr[k] = BpFrame{G[k]->corrcal, G[k]->ratio, nullptr};
+  }
+  if (!pairs.empty()) {
+    b.nfr = (int)pairs.size();
+    for (size_t i = 0; i < pairs.size(); i++) b.fr[i] = bf[pairs[i]];
+    GF_LAUNCH(c, launch_bp_pairs(b, c->bp_warps, st));
+  }
+  if (!singles.empty()) {
+    b.nfr = (int)singles.size();
+    for (size_t i = 0; i < singles.size(); i++) b.fr[i] = bf[singles[i]];
     GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
   }
   ImgFrames u{};

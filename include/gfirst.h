@@ -279,17 +279,18 @@ void gf_batch_destroy(gf_batch* b);
  * the kernels are launched directly, frame by frame.  Asynchronous. */
 gf_status gf_batch_iterate(gf_batch* b, int32_t n, int32_t use_graph);
 gf_status gf_batch_synchronize(gf_batch* b);
-/* With fused = 1 or 2, mode-1 frames that share geometry, subset count,
- * storage, filters, back-projector form and tile shapes advance as fused
- * groups of up to 16: every stage of a sub-iteration (forward PSF,
- * projection + ratio, back projection, update) is one kernel launch over the
- * group's frames, each frame keeping its own data and results (the same as
- * alone, bit for bit).  With fused = 1, a group whose frames' normalization
- * masks are equal (checked on the device) and whose back projector is in
- * the per-view form back-projects two frames per warp, sharing the per-view
- * geometry and the staged mask rows; fused = 2 keeps one frame per warp.
- * Other frames run on their own.  0 turns fusing off.  Takes effect at the
- * next iterate. */
+/* With fused = 1 or 2, mode-1 frames that share geometry, storage, filters,
+ * back-projector form and tile shapes advance as fused groups of up to 16,
+ * whatever their subset counts: step s of a group's iteration runs the
+ * frames that have a subset s, each at its own subset s, and every stage
+ * (forward PSF, projection + ratio, back projection, update) is one kernel
+ * launch over those frames, each frame keeping its own data and results (the
+ * same as alone, bit for bit).  With fused = 1, frames of a group with the
+ * same subset count and equal normalization masks (checked on the device),
+ * back projector in the per-view form, back-project two per warp, sharing
+ * the per-view geometry and the staged mask rows; fused = 2 keeps one frame
+ * per warp.  Other frames run on their own.  0 turns fusing off.  Takes
+ * effect at the next iterate. */
 gf_status gf_batch_set_fused(gf_batch* b, int32_t fused);
 /* Units the batch runs (fused groups and single frames), the size of the
  * largest group and the frame pairs back-projected together, as they stand

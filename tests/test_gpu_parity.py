@@ -845,12 +845,12 @@ def test_batch_matches_frames_run_alone(gf, graph):
 
 @pytest.mark.parametrize("graph,pairs", [(True, True), (False, True), (True, False)])
 def test_fused_batch_matches_frames_run_alone(gf, graph, pairs):
-    """Fused groups (gf_batch_set_fused): the four mode-1 frames with two
-    subsets run every stage as one launch over the group (with pairs, their
-    back projection two frames per warp, the normalization being the same);
-    the frame with three subsets and the mode-2 frame run on their own.
-    Every frame's images equal the same frame run alone, bit for bit (the
-    same arithmetic per frame)."""
+    """Fused groups (gf_batch_set_fused): the five mode-1 frames (four with
+    two subsets, one with three) run every stage as one launch over the
+    frames that have the step's subset (with pairs, the four two-subset
+    frames back-project two per warp, the normalization being the same); the
+    mode-2 frame runs on its own.  Every frame's images equal the same frame
+    run alone, bit for bit (the same arithmetic per frame)."""
     d = parsed("tinyb")
     specs = [(1, 2), (1, 3), (1, 2), (2, 2), (1, 2), (1, 2)]
     frames = _frames(gf, specs)
@@ -870,17 +870,46 @@ def test_fused_batch_matches_frames_run_alone(gf, graph, pairs):
         alone.append((a.image(0), a.image(1)))
     b = gf.Batch([r for _, r in frames])
     b.set_fused(True, pairs=pairs)
-    assert b.groups() == (3, 4, 2 if pairs else 0)
+    assert b.groups() == (2, 5, 2 if pairs else 0)
     l0 = sum(c.launches() for c, _ in frames)
     b.iterate(1, graph=graph)
     b.iterate(2, graph=graph)
     b.sync()
-    # per iteration: the group's 2 sub-iterations x 5 launches, plus the singles'
     launches = sum(c.launches() for c, _ in frames) - l0
     assert launches > 0
     for k, ((_, r), (a0, a1)) in enumerate(zip(frames, alone)):
         assert np.array_equal(r.image(0), a0), k
         assert np.array_equal(r.image(1), a1), k
+    b.close()
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_fused_mixed_subset_counts_match_frames_alone(gf, graph):
+    """One fused group of seven frames with 2, 3, 4 and 5 subsets (12 angles:
+    the five-subset frame's subsets hold 3 or 2 angles): step s launches each
+    stage once over the frames that have a subset s, each at its own angles;
+    frames with the same subset count pair up in the back projector.  Every
+    frame equals the same frame run alone, bit for bit."""
+    d = parsed("tinyb")
+    g = gf.Geometry(*case("tinyb"))
+    counts = [2, 3, 4, 2, 5, 4, 3]
+    frames = []
+    for k, nsub in enumerate(counts):
+        c = gf.Context(g, nsub=nsub)
+        r = gf.Recon(c, 1, niter=2)
+        r.load(dsino=np.roll(d["dsino"], 5 * k), norm=d["norm"])
+        frames.append((c, r))
+    b = gf.Batch([r for _, r in frames])
+    b.set_fused(True)
+    assert b.groups() == (1, 7, 3)  # pairs of the 2-, 3- and 4-subset frames
+    b.iterate(2, graph=graph)
+    b.sync()
+    for k, nsub in enumerate(counts):
+        c = gf.Context(g, nsub=nsub)
+        a = gf.Recon(c, 1, niter=2)
+        a.load(dsino=np.roll(d["dsino"], 5 * k), norm=d["norm"])
+        a.iterate(2)
+        assert np.array_equal(frames[k][1].image(0), a.image(0)), (k, nsub)
     b.close()
 
 
@@ -909,7 +938,9 @@ def test_fused_groups_hold_at_most_sixteen_frames(gf):
 
 
 def test_fused_pairs_need_equal_normalizations(gf):
-    """Frames whose normalization masks differ are fused but not paired."""
+    """Frames whose normalization masks differ are fused but not paired: of
+    three frames, the two with the same normalization pair up and the third
+    goes alone."""
     d = parsed("tinyb")
     g = gf.Geometry(*case("tinyb"))
     frames = []
@@ -923,7 +954,7 @@ def test_fused_pairs_need_equal_normalizations(gf):
         frames.append((c, r, norm))
     b = gf.Batch([r for _, r, _ in frames])
     b.set_fused(True)
-    assert b.groups() == (1, 3, 0)
+    assert b.groups() == (1, 3, 1)
     b.iterate(2)
     b.sync()
     for c, r, norm in frames:
