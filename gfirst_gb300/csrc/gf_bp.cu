@@ -257,9 +257,8 @@ __device__ __forceinline__ void bp_column(const BpArgs& a, int rmax) {
   }
   // per angle: radial texels, weight and yrot (GFIRST_GPU_Kernels.cu:136-147)
   const float xv = __fsub_rn((float)ix, g.resm), yv = __fsub_rn((float)iy, g.resm);
-  const int na = F.na;
-  for (int tl = lane; tl < na; tl += 32) {
-    const float2 sc = g.trig[subset_angle(F.subset, F.nsub, tl)];
+  for (int tl = lane; tl < a.na; tl += 32) {
+    const float2 sc = g.trig[subset_angle(g, a.subset, tl)];
     const float xrot = __fadd_rn(__fmul_rn(xv, sc.y), __fmul_rn(yv, sc.x));
     const float yrot = __fadd_rn(__fmul_rn(-xv, sc.x), __fmul_rn(yv, sc.y));
     const float x = __fadd_rn(__fadd_rn(g.radm, __fmul_rn(xrot, g.fx_bp)), 0.5f);
@@ -291,7 +290,7 @@ __device__ __forceinline__ void bp_column(const BpArgs& a, int rmax) {
     switch ((sg.nplanes + 2 + 31) >> 5) {
 #define GF_SEG(N) \
   case N:         \
-    if constexpr (N <= Q + 1) segment_views<Q, N, FAST>(acc, fiz, cc, my, rows, sg, na, g.nzs, lane); \
+    if constexpr (N <= Q + 1) segment_views<Q, N, FAST>(acc, fiz, cc, my, rows, sg, a.na, g.nzs, lane); \
     break;
       GF_SEG(1) GF_SEG(2) GF_SEG(3) GF_SEG(4) GF_SEG(5) GF_SEG(6) GF_SEG(7) GF_SEG(8) GF_SEG(9)
 #undef GF_SEG
@@ -454,9 +453,8 @@ __device__ __forceinline__ void bp_column_pair(const BpArgs& a, int rmax) {
   rc += a.pad_lo;
   // per angle: radial texels, weight and yrot (GFIRST_GPU_Kernels.cu:136-147)
   const float xv = __fsub_rn((float)ix, g.resm), yv = __fsub_rn((float)iy, g.resm);
-  const int na = FA.na;  // the pair's frames share their subset
-  for (int tl = lane; tl < na; tl += 32) {
-    const float2 sc = g.trig[subset_angle(FA.subset, FA.nsub, tl)];
+  for (int tl = lane; tl < a.na; tl += 32) {
+    const float2 sc = g.trig[subset_angle(g, a.subset, tl)];
     const float xrot = __fadd_rn(__fmul_rn(xv, sc.y), __fmul_rn(yv, sc.x));
     const float yrot = __fadd_rn(__fmul_rn(-xv, sc.x), __fmul_rn(yv, sc.y));
     const float x = __fadd_rn(__fadd_rn(g.radm, __fmul_rn(xrot, g.fx_bp)), 0.5f);
@@ -485,7 +483,7 @@ __device__ __forceinline__ void bp_column_pair(const BpArgs& a, int rmax) {
     switch ((sg.nplanes + 2 + 31) >> 5) {
 #define GF_SEGP(N) \
   case N:          \
-    if constexpr (N <= Q + 1) segment_views_pair<Q, N>(accA, accB, ccA, ccB, my, rr, rc, sg, na, lane); \
+    if constexpr (N <= Q + 1) segment_views_pair<Q, N>(accA, accB, ccA, ccB, my, rr, rc, sg, a.na, lane); \
     break;
       GF_SEGP(1) GF_SEGP(2) GF_SEGP(3) GF_SEGP(4) GF_SEGP(5) GF_SEGP(6) GF_SEGP(7) GF_SEGP(8) GF_SEGP(9)
 #undef GF_SEGP
@@ -508,24 +506,22 @@ __global__ void __launch_bounds__(256) __maxnreg__(bp_pair_regs<STORE>) bp_pair_
   bp_column_pair<Q, STORE>(a, rmax);
 }
 
-// A frame's subset: angles subset + l*nsub, l < na, all inside [0, nang); its
-// table fits the launch's shared memory (na <= BpArgs::na).
-static bool subset_ok(const BpArgs& a, const BpFrame& F) {
-  return F.nsub >= 1 && F.subset >= 0 && F.subset < F.nsub && F.na >= 1 && F.na <= a.na &&
-         F.na == (a.g.nang - F.subset + F.nsub - 1) / F.nsub;
+// One launch serves one subset: every frame takes angles subset + l*g.nsub,
+// l < na (the frames of a fused group with another subset count get a launch
+// of their own), which keeps the subset a launch constant in the kernels.
+static bool subset_ok(const BpArgs& a) {
+  return a.g.nsub >= 1 && a.subset >= 0 && a.subset < a.g.nsub && a.na >= 1 &&
+         a.na == (a.g.nang - a.subset + a.g.nsub - 1) / a.g.nsub;
 }
 
 cudaError_t launch_bp_pairs(const BpArgs& a, int warps, cudaStream_t st) {
+  if (!subset_ok(a)) return cudaErrorInvalidValue;
   if (warps < 1 || warps > 8) return cudaErrorInvalidValue;
   if (!a.fast || a.pad_lo < 0 || a.rbuf < a.pad_lo + a.g.nzs + 2) return cudaErrorInvalidValue;
   const int npairs = a.nfr / 2;
   if (npairs < 1 || 2 * npairs != a.nfr || a.nfr > kMaxFrames) return cudaErrorInvalidValue;
-  for (int f = 0; f < a.nfr; f++) {
+  for (int f = 0; f < a.nfr; f++)
     if (!a.fr[f].corrcal || !a.fr[f].numer || (!a.ratio && !a.fr[f].denom)) return cudaErrorInvalidValue;
-    if (!subset_ok(a, a.fr[f])) return cudaErrorInvalidValue;
-    const BpFrame& A = a.fr[f & ~1];
-    if (a.fr[f].subset != A.subset || a.fr[f].nsub != A.nsub) return cudaErrorInvalidValue;  // a pair shares its subset
-  }
   const int Q = a.g.nzp / 32;
   const int rmax = a.rbuf;
   dim3 grid((a.g.res * a.g.res + warps - 1) / warps, npairs);
@@ -592,14 +588,13 @@ static void (*bp_entry(bool fast))(BpArgs, int) {
 
 cudaError_t launch_bp(const BpArgs& a, int warps, cudaStream_t st) {
   if (warps < 1 || warps > 8) return cudaErrorInvalidValue;
+  if (!subset_ok(a)) return cudaErrorInvalidValue;
   const int Q = a.g.nzp / 32;
   if (a.fast && (a.pad_lo < 0 || a.rbuf < a.pad_lo + a.g.nzs + 2)) return cudaErrorInvalidValue;
   const int rmax = a.fast ? a.rbuf : a.g.nzs + 2;
   if (a.nfr < 0 || a.nfr > kMaxFrames) return cudaErrorInvalidValue;
-  for (int f = 0; f < (a.nfr > 1 ? a.nfr : 1); f++) {
+  for (int f = 0; f < (a.nfr > 1 ? a.nfr : 1); f++)
     if (!a.fr[f].corrcal || !a.fr[f].numer || (!a.ratio && !a.fr[f].denom)) return cudaErrorInvalidValue;
-    if (!subset_ok(a, a.fr[f])) return cudaErrorInvalidValue;
-  }
   dim3 grid((a.g.res * a.g.res + warps - 1) / warps, a.nfr > 1 ? a.nfr : 1);
   size_t smem = (size_t)warps * (a.na * sizeof(int4) + rmax * sizeof(float2));
   void (*k)(BpArgs, int) = nullptr;

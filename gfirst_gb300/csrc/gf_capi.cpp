@@ -123,14 +123,12 @@ FpArgs gf_ctx::fp_args(int subset, const float* img_zfast) const {
 BpArgs gf_ctx::bp_args(int subset, const void* cc, float* numer, float* denom, int storage) const {
   BpArgs b{};
   b.g = dg;
+  b.subset = subset;
   b.na = plan.sub_nang[subset];
   b.nfr = 1;
   b.fr[0].corrcal = cc;
   b.fr[0].numer = numer;
   b.fr[0].denom = denom;
-  b.fr[0].subset = subset;
-  b.fr[0].nsub = plan.nsub;
-  b.fr[0].na = plan.sub_nang[subset];
   b.storage = storage;
   b.fast = bp_form == GF_BP_PER_VIEW ? 1 : 0;
   b.pad_lo = bpp.pad_lo;

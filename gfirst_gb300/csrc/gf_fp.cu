@@ -35,9 +35,13 @@ __global__ void __launch_bounds__(512) fp_kernel(const FpArgs a) {
   const DevGeom& g = a.g;
   const FpFrame& F = a.fr[blockIdx.z];
   const int ird = blockIdx.x, tl = blockIdx.y;
-  if (tl >= F.na) return;  // a frame with fewer angles in its subset than the launch's largest
+  // a frame with fewer angles in its subset than the launch's largest: its
+  // surplus blocks march no rays and write nothing (an early return here
+  // costs the kernel 13 registers)
+  const bool active = tl < F.na;
+  const int lam_end = active ? g.lam1 : g.lam0 - 1;
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int theta = subset_angle(F.subset, F.nsub, tl);
+  const int theta = subset_angle(F.subset, F.nsub, active ? tl : 0);
   const float2 sc = g.trig[theta];
   const float sn = sc.x, cs = sc.y;
   // GFIRST_GPU_Kernels.cu:79-87 (fac = RES/NPT = 1 makes dx = sin, dy = -cos exactly)
@@ -60,7 +64,7 @@ __global__ void __launch_bounds__(512) fp_kernel(const FpArgs a) {
   for (int j = 0; j < R; j++) acc[j] = 0.f;
 
   const int npad = cw - NZS;
-  for (int lb = g.lam0; lb <= g.lam1; lb += lc) {
+  for (int lb = g.lam0; lb <= lam_end; lb += lc) {
     const int nl = min(lc, g.lam1 - lb + 1);
     for (int l = tid; l < nl; l += nt) {
       const float fl = (float)(lb + l);
@@ -113,7 +117,7 @@ __global__ void __launch_bounds__(512) fp_kernel(const FpArgs a) {
     __syncthreads();
   }
 
-  if (run.x < 0) return;
+  if (run.x < 0 || !active) return;
   const DevSeg sg = g.seg[run.x];
   const size_t base = ((size_t)tl * g.nrad + ird) * g.PS;
   const float2 sentinel = make_float2(-1000.f, -1000.f);

@@ -163,11 +163,11 @@ namespace gf {
 bool fusable(const gf_recon* a, const gf_recon* b);
 // One sub-iteration of every frame of a fused group, all at the same subset
 // index s, each at subset s of its own subset count: the forward PSF,
-// projection + ratio, back projection and update are one launch each over
-// the nfr <= kMaxFrames frames, on stream st (the group's: its first
-// member's, which need not take part in every step) with the first
-// frame's tables.  Advances every frame's cursor.  cls: frames with the same
-// class >= 0 (same subset count and normalization mask; per-view back
-// projector) back-project two per warp.
+// projection + ratio and update are one launch each over the nfr <=
+// kMaxFrames frames, the back projection one launch per subset count among
+// them, on stream st (the group's: its first member's, which need not take
+// part in every step) with the first frame's tables.  Advances every frame's
+// cursor.  cls: frames with the same class >= 0 (same subset count and
+// normalization mask; per-view back projector) back-project two per warp.
 gf_status fused_subiteration(gf_recon* const* G, int nfr, const int* cls, cudaStream_t st);
 }  // namespace gf

@@ -21,9 +21,9 @@ struct Taps5 { float c[5]; };
 // One launch may serve several frames of one geometry (a fused group of a
 // batch): every per-frame buffer sits in a table of kMaxFrames entries passed
 // by value, the launch has one grid slice per frame, and a block takes its
-// frame's entry.  Frames may differ in subset count: each entry names its
-// frame's subset (angles subset + l*nsub, l < na).  A single-frame launch
-// fills entry 0.
+// frame's entry.  In the forward projector the frames may differ in subset
+// count (each entry names its frame's subset); the back projector's frames
+// share one.  A single-frame launch fills entry 0.
 constexpr int kMaxFrames = 16;
 
 // ---- forward projector (gf_fp.cu) ----
@@ -50,11 +50,11 @@ struct BpFrame {
   const void* corrcal;     // subset layout (corr, calib) pairs
   float* numer;            // z-fast
   float* denom;            // z-fast
-  int subset, nsub, na;    // as FpFrame
 };
+// The back projector's launches serve one subset (of g.nsub) for all frames.
 struct BpArgs {
-  DevGeom g;               // g.nsub unused: each frame names its own
-  int na;                  // the most angles of any frame's subset (shared-memory tables)
+  DevGeom g;
+  int subset, na;          // na: angles in this subset
   int nfr;                 // frames in this launch (grid y); 0 is taken as 1
   BpFrame fr[kMaxFrames];
   int storage;             // corrcal pair type, as FpArgs::storage

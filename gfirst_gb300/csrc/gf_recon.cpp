@@ -189,48 +189,51 @@ gf_status fused_subiteration(gf_recon* const* G, int nfr, const int* cls, cudaSt
   FpArgs a = c->fp_args(s, nullptr);
   a.nfr = nfr;
   a.storage = r0->p.storage;
-  std::vector<BpFrame> bf(nfr);
-  int na_max = 0;
   for (int k = 0; k < nfr; k++) {
     const Plan& pk = G[k]->ctx->plan;
     const int64_t off = pk.sub_off[s];
-    const int na = pk.sub_nang[s];
-    a.fr[k] = FpFrame{G[k]->psf, G[k]->dbg[0] + off, G[k]->cal + off, G[k]->corrcal, nullptr, s, pk.nsub, na};
-    bf[k] = BpFrame{G[k]->corrcal, G[k]->ratio, nullptr, s, pk.nsub, na};
-    na_max = std::max(na_max, na);
+    a.fr[k] = FpFrame{G[k]->psf, G[k]->dbg[0] + off, G[k]->cal + off, G[k]->corrcal, nullptr, s, pk.nsub,
+                      pk.sub_nang[s]};
   }
   GF_LAUNCH(c, launch_fp(a, c->fps, st));
-  BpArgs b = c->bp_args(s, r0->corrcal, r0->ratio, nullptr, r0->p.storage);
-  b.ratio = 1;
-  b.na = na_max;
-  // frames of one class (same subset count and normalization mask) share a
-  // warp per column two by two; the rest go alone
-  std::vector<int> pairs, singles;
-  std::vector<bool> used(nfr, false);
-  for (int k = 0; k < nfr; k++) {
-    if (used[k]) continue;
-    used[k] = true;
-    int j = -1;
-    if (b.fast && cls && cls[k] >= 0)
-      for (int m = k + 1; m < nfr && j < 0; m++)
-        if (!used[m] && cls[m] == cls[k]) j = m;
-    if (j >= 0) {
-      used[j] = true;
-      pairs.push_back(k);
-      pairs.push_back(j);
-    } else {
-      singles.push_back(k);
+  // the back projector keeps the subset a launch constant: one launch per
+  // subset count among the frames; within it, frames of one class (same
+  // normalization mask) share a warp per column two by two
+  std::vector<bool> done(nfr, false);
+  for (int k0 = 0; k0 < nfr; k0++) {
+    if (done[k0]) continue;
+    const Plan& pl = G[k0]->ctx->plan;
+    BpArgs b = c->bp_args(s, nullptr, nullptr, nullptr, r0->p.storage);
+    b.g.nsub = pl.nsub;
+    b.na = pl.sub_nang[s];
+    b.ratio = 1;
+    std::vector<int> pairs, singles;
+    for (int k = k0; k < nfr; k++) {
+      if (done[k] || G[k]->ctx->plan.nsub != pl.nsub) continue;
+      done[k] = true;
+      int j = -1;
+      if (b.fast && cls && cls[k] >= 0)
+        for (int m = k + 1; m < nfr && j < 0; m++)
+          if (!done[m] && cls[m] == cls[k]) j = m;
+      if (j >= 0) {
+        done[j] = true;
+        pairs.push_back(k);
+        pairs.push_back(j);
+      } else {
+        singles.push_back(k);
+      }
     }
-  }
-  if (!pairs.empty()) {
-    b.nfr = (int)pairs.size();
-    for (size_t i = 0; i < pairs.size(); i++) b.fr[i] = bf[pairs[i]];
-    GF_LAUNCH(c, launch_bp_pairs(b, c->bp_warps, st));
-  }
-  if (!singles.empty()) {
-    b.nfr = (int)singles.size();
-    for (size_t i = 0; i < singles.size(); i++) b.fr[i] = bf[singles[i]];
-    GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
+    if (!pairs.empty()) {
+      b.nfr = (int)pairs.size();
+      for (size_t i = 0; i < pairs.size(); i++) b.fr[i] = BpFrame{G[pairs[i]]->corrcal, G[pairs[i]]->ratio, nullptr};
+      GF_LAUNCH(c, launch_bp_pairs(b, c->bp_warps, st));
+    }
+    if (!singles.empty()) {
+      b.nfr = (int)singles.size();
+      for (size_t i = 0; i < singles.size(); i++)
+        b.fr[i] = BpFrame{G[singles[i]]->corrcal, G[singles[i]]->ratio, nullptr};
+      GF_LAUNCH(c, launch_bp(b, c->bp_warps, st));
+    }
   }
   ImgFrames u{};
   for (int k = 0; k < nfr; k++) u.fr[k] = ImgFrame{G[k]->ratio, nullptr, G[k]->img[0]};

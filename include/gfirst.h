@@ -282,10 +282,10 @@ gf_status gf_batch_synchronize(gf_batch* b);
 /* With fused = 1 or 2, mode-1 frames that share geometry, storage, filters,
  * back-projector form and tile shapes advance as fused groups of up to 16,
  * whatever their subset counts: step s of a group's iteration runs the
- * frames that have a subset s, each at its own subset s, and every stage
- * (forward PSF, projection + ratio, back projection, update) is one kernel
- * launch over those frames, each frame keeping its own data and results (the
- * same as alone, bit for bit).  With fused = 1, frames of a group with the
+ * frames that have a subset s, each at its own subset s; the forward PSF,
+ * projection + ratio and update are one kernel launch over those frames and
+ * the back projection one launch per subset count among them, each frame
+ * keeping its own data and results (the same as alone, bit for bit).  With fused = 1, frames of a group with the
  * same subset count and equal normalization masks (checked on the device),
  * back projector in the per-view form, back-project two per warp, sharing
  * the per-view geometry and the staged mask rows; fused = 2 keeps one frame
