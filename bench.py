@@ -495,6 +495,14 @@ def run_gpu(args) -> int:
             read(0)
             seq_ms.append(1000 * (time.perf_counter() - ts))
         dt_seq = max_over_ranks(time.perf_counter() - t0, dist)
+        # warm-up of the pipelined loop itself (3 steps), then the timed loop
+        # from an empty pipeline
+        issue(0)
+        for k in range(3):
+            if k + 1 < 3:
+                issue(k + 1)
+            read(k)
+        torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
         step_ms = []  # host clock from one image's read-back to the next

@@ -21,6 +21,28 @@ __device__ __forceinline__ void img_st(__half* p, float v) { *p = __float2half_r
 __device__ __forceinline__ void img_st(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
 
 // ---- separable XY Gaussian, GFIRST_GPU_Kernels.cu:332-358 -----------------
+// Stages the 16x16-column tile around output columns [x0, x0+8) x [y0, y0+8)
+// at this lane's slice z into S, 0 outside the image (or everywhere when
+// !zok): warp ty loads halo columns ty and ty + 8 of every halo row, so the
+// two columns' bounds and offsets are computed once and each row is one
+// stride further.
+template <class T>
+__device__ __forceinline__ void stage_halo(float (&S)[16][16][32], const T* __restrict__ in, bool zok, int z, int x0,
+                                           int y0, int ty, int lane, int RES, int NZP) {
+  const int xa = x0 - 4 + ty, xb = x0 + 4 + ty;  // xb >= 4
+  const bool oka = zok && xa >= 0 && xa < RES, okb = zok && xb < RES;
+  const long long rs = (long long)RES * NZP;
+  const long long ra = ((long long)(y0 - 4) * RES + xa) * NZP + z;  // element offset at halo row 0, column xa
+  const long long rb = ra + 8LL * NZP;                               // column xb
+#pragma unroll
+  for (int yy = 0; yy < 16; yy++) {
+    const int y = y0 - 4 + yy;
+    const bool oky = y >= 0 && y < RES;
+    S[yy][ty][lane] = (oky && oka) ? img_ld(in + (ra + yy * rs)) : 0.f;
+    S[yy][ty + 8][lane] = (oky && okb) ? img_ld(in + (rb + yy * rs)) : 0.f;
+  }
+}
+
 // conv_xy9 runs it on an 8x8-column, 32-slice tile staged with a 4-column
 // halo in S: the y pass is zero-padded; the x pass runs only for
 // 3 < x < RES-4 and border columns output the raw input.  Thread (row ty,
@@ -64,12 +86,7 @@ __global__ void __launch_bounds__(256) conv_xy_kernel(const DevGeom g, const Img
   const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int x0 = blockIdx.x * 8, y0 = blockIdx.y * 8, z = (blockIdx.z - f * nzc) * 32 + lane;
   const int RES = g.res, NZP = g.nzp;
-#pragma unroll 8
-  for (int c = ty; c < 256; c += 8) {
-    const int yy = c >> 4, xx = c & 15;
-    const int y = y0 - 4 + yy, x = x0 - 4 + xx;
-    S[yy][xx][lane] = (y >= 0 && y < RES && x >= 0 && x < RES) ? img_ld(in + ((size_t)y * RES + x) * NZP + z) : 0.f;
-  }
+  stage_halo(S, in, true, z, x0, y0, ty, lane, RES, NZP);
   __syncthreads();
   float v[8];
   conv_xy9(S, ty, lane, x0, RES, G, v);
@@ -127,11 +144,16 @@ cudaError_t launch_voxel_ratio(const DevGeom& g, const float* numer, const float
 // column (y=0, x=0), which takes the rule of slice z-1; reads past the last
 // slice are 0.  The rule is applied centred on the voxel itself; m2..p2 are
 // the inputs at slices z-2..z+2, already 0 outside [0, NZS).
-__device__ __forceinline__ float zrule(float m2, float m1, float c0, float p1, float p2, int K, int NZS,
-                                       const Taps5& g) {
-  if (K == 0) return __fadd_rn(__fmul_rn(0.5f, c0), __fmul_rn(0.5f, p1));
-  if (K == NZS - 1) return __fadd_rn(__fmul_rn(0.5f, m1), __fmul_rn(0.5f, c0));
-  if (K == 1 || K == NZS - 2)
+// Which rule slice K takes, in the reference's order of tests: 0 the first
+// slice's 2 taps, 1 the last slice's 2 taps, 2 the 3 taps of the second and
+// second-to-last slices, 3 the 5-tap Gaussian.
+__device__ __forceinline__ int zrule_of(int K, int NZS) {
+  return K == 0 ? 0 : (K == NZS - 1 ? 1 : ((K == 1 || K == NZS - 2) ? 2 : 3));
+}
+__device__ __forceinline__ float zrule(float m2, float m1, float c0, float p1, float p2, int rule, const Taps5& g) {
+  if (rule == 0) return __fadd_rn(__fmul_rn(0.5f, c0), __fmul_rn(0.5f, p1));
+  if (rule == 1) return __fadd_rn(__fmul_rn(0.5f, m1), __fmul_rn(0.5f, c0));
+  if (rule == 2)
     return __fadd_rn(__fadd_rn(__fmul_rn(0.333f, m1), __fmul_rn(0.333f, c0)), __fmul_rn(0.333f, p1));
   float v = __fmul_rn(g.c[0], m2);
   v = __fadd_rn(v, __fmul_rn(g.c[1], m1));
@@ -153,7 +175,7 @@ __device__ __forceinline__ float zrule(float m2, float m1, float c0, float p1, f
 // a CTA reads image values of its own outputs only and the in-place update
 // needs no ordering between CTAs.  Grid z runs over (frame, chunk).
 template <class T>
-__global__ void __launch_bounds__(256) update_kernel(const DevGeom g, const ImgFrames fr, const Taps9 G,
+__global__ void __launch_bounds__(256, 6) update_kernel(const DevGeom g, const ImgFrames fr, const Taps9 G,
                                                      const Taps5 t5, int cs) {
   __shared__ float S[16][16][32];
   const int nzc = (g.nzp + cs - 1) / cs;
@@ -164,13 +186,7 @@ __global__ void __launch_bounds__(256) update_kernel(const DevGeom g, const ImgF
   const int x0 = blockIdx.x * 8, y0 = blockIdx.y * 8;
   const int z = (blockIdx.z - f * nzc) * cs - 2 + lane;
   const int RES = g.res, NZP = g.nzp, NZS = g.nzs;
-  const bool zload = z >= 0 && z < NZP;
-#pragma unroll 8
-  for (int c = ty; c < 256; c += 8) {
-    const int yy = c >> 4, xx = c & 15;
-    const int y = y0 - 4 + yy, x = x0 - 4 + xx;
-    S[yy][xx][lane] = (zload && y >= 0 && y < RES && x >= 0 && x < RES) ? ratio[((size_t)y * RES + x) * NZP + z] : 0.f;
-  }
+  stage_halo(S, ratio, z >= 0 && z < NZP, z, x0, y0, ty, lane, RES, NZP);
   __syncthreads();
   float v[8];
   conv_xy9(S, ty, lane, x0, RES, G, v);
@@ -178,6 +194,7 @@ __global__ void __launch_bounds__(256) update_kernel(const DevGeom g, const ImgF
   if (y >= RES) return;  // whole warp
   const bool out_lane = lane >= 2 && lane < cs + 2 && z < NZP;
   const bool zin = z >= 0 && z < NZS;
+  const int rule = zrule_of(z, NZS);
 #pragma unroll
   for (int xo = 0; xo < 8; xo++) {
     const int x = x0 + xo;
@@ -187,8 +204,8 @@ __global__ void __launch_bounds__(256) update_kernel(const DevGeom g, const ImgF
     const float c0 = zin ? v[xo] : 0.f;
     const float m1 = __shfl_up_sync(0xffffffffu, c0, 1), m2 = __shfl_up_sync(0xffffffffu, c0, 2);
     const float p1 = __shfl_down_sync(0xffffffffu, c0, 1), p2 = __shfl_down_sync(0xffffffffu, c0, 2);
-    const int K = (x == 0 && y == 0) ? z - 1 : z;
-    const float prod = __fmul_rn(iv, zrule(m2, m1, c0, p1, p2, K, NZS, t5));
+    // column (0, 0) takes slice z-1's rule
+    const float prod = __fmul_rn(iv, zrule(m2, m1, c0, p1, p2, (x == 0 && y == 0) ? zrule_of(z - 1, NZS) : rule, t5));
     const float up = __shfl_down_sync(0xffffffffu, prod, 1);  // slice z + 1
     const float dn = __shfl_up_sync(0xffffffffu, prod, 1);    // slice z - 1
     if (out_lane) img_st(img + o, z >= NZS ? 0.f : (z == 0 ? up : (z == NZS - 1 ? dn : prod)));
