@@ -30,6 +30,7 @@ Prints one JSON line (rank 0).
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -470,6 +471,11 @@ def run_gpu(args) -> int:
         for k in range(2):  # warm-up: device staging, the geometry projection
             issue(k, wait=True)
             read(k)
+        # a long-running host keeps the garbage collector off its set-up's
+        # objects: a full collection over the interpreter's and torch's
+        # objects stalls the issuing thread for tens of milliseconds
+        gc.collect()
+        gc.freeze()
         # where a sequential step's time goes (host clock): the synchronous load,
         # queueing the iterations, then waiting for them and reading the image
         phases = {"load_ms": [], "queue_ms": [], "wait_read_ms": []}
@@ -532,6 +538,7 @@ def run_gpu(args) -> int:
                               "step_ms": [round(x, 2) for x in seq_ms],
                               "path": "gf_recon_load + gf_recon_iterate(2) + gf_recon_get_image, one "
                                       "reconstruction, each step after the previous one"}}
+        gc.unfreeze()
         for rr in recs:
             rr.close()
         gf.lib().gf_host_free(hp)
