@@ -318,6 +318,7 @@ void gf_destroy(gf_ctx* c) {
   // wait for the context's work, then return its memory on a stream of the
   // library's own, so a caller's stream set by gf_set_stream is not needed
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
   cudaGetLastError();
   cudaStream_t fs = nullptr;
   if (cudaStreamCreateWithFlags(&fs, cudaStreamNonBlocking) != cudaSuccess) {
@@ -328,10 +329,7 @@ void gf_destroy(gf_ctx* c) {
   cudaStreamSynchronize(fs);
   if (fs) cudaStreamDestroy(fs);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
-  if (c->copy_stream) {
-    cudaStreamSynchronize(c->copy_stream);
-    cudaStreamDestroy(c->copy_stream);
-  }
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   delete c;
 }
 
