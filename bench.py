@@ -437,38 +437,40 @@ def run_gpu(args) -> int:
     if args.e2e_steps > 0:
         # end to end through the public C-ABI with pinned host buffers: every
         # step uploads its sinogram + normalization, runs the 32 sub-iterations
-        # and reads the scaled image back.  Two reconstructions of one context
-        # alternate: step k+1's upload is queued (gf_recon_load_async, on the
-        # context's copy stream, overlapping step k's iterations) before step
-        # k's image is read back (also on the copy stream, after step k's own
-        # work only); the one-reconstruction sequential loop is reported
-        # beside it.
+        # and reads the scaled image back.  Three reconstructions of one
+        # context take the steps in turn: steps k+1 and k+2 are queued
+        # (gf_recon_load_async, their uploads on the context's copy stream,
+        # overlapping step k's iterations) before step k's image is read back
+        # (also on the copy stream, after step k's own work only), so an
+        # upload has two steps' iterations to finish in; the
+        # one-reconstruction sequential loop is reported beside it.
+        NB = 3  # reconstructions (and host buffer sets) in rotation
         n2 = 2 * ndata
         per = n2 + ndata + nvox
         hp = gf.ctypes.c_void_p()
-        gf._ck(gf.lib().gf_host_alloc(gf.ctypes.c_size_t(2 * per * 4), gf.ctypes.byref(hp)))
-        buf = np.ctypeslib.as_array(gf.ctypes.cast(hp, gf.ctypes.POINTER(gf.ctypes.c_float)), (2 * per,))
+        gf._ck(gf.lib().gf_host_alloc(gf.ctypes.c_size_t(NB * per * 4), gf.ctypes.byref(hp)))
+        buf = np.ctypeslib.as_array(gf.ctypes.cast(hp, gf.ctypes.POINTER(gf.ctypes.c_float)), (NB * per,))
         host = []
-        for i in range(2):
+        for i in range(NB):
             b = buf[i * per:(i + 1) * per]
             hs, hn, ho = b[:n2], b[n2:n2 + ndata], b[n2 + ndata:]
             hs[:] = dsino
             hn[:] = norm
             host.append((hs, hn, ho))
-        recs = [gf.Recon(ctx, 1, niter=NITER), gf.Recon(ctx, 1, niter=NITER)]
+        recs = [gf.Recon(ctx, 1, niter=NITER) for _ in range(NB)]
         ptr = lambda a: a.ctypes.data_as(gf.ctypes.c_void_p)  # noqa: E731
         lib = gf.lib()
 
         def issue(k, wait=False):
-            r, (hs, hn, _) = recs[k % 2], host[k % 2]
+            r, (hs, hn, _) = recs[k % NB], host[k % NB]
             fn = lib.gf_recon_load if wait else lib.gf_recon_load_async
             gf._ck(fn(r.h, None, ptr(hs), None, ptr(hn), None, gf.ctypes.c_int64(0)))
             r.iterate(NITER)
 
         def read(k):
-            gf._ck(lib.gf_recon_get_image(recs[k % 2].h, 0, 1, ptr(host[k % 2][2])))
+            gf._ck(lib.gf_recon_get_image(recs[k % NB].h, 0, 1, ptr(host[k % NB][2])))
 
-        for k in range(2):  # warm-up: device staging, the geometry projection
+        for k in range(NB):  # warm-up: device staging, the geometry projection
             issue(k, wait=True)
             read(k)
         # a long-running host keeps the garbage collector off its set-up's
@@ -501,26 +503,28 @@ def run_gpu(args) -> int:
             read(0)
             seq_ms.append(1000 * (time.perf_counter() - ts))
         dt_seq = max_over_ranks(time.perf_counter() - t0, dist)
+
+        def pipelined(nsteps, times=None):
+            ts = time.perf_counter()
+            for k in range(min(NB - 1, nsteps)):
+                issue(k)
+            for k in range(nsteps):
+                if k + NB - 1 < nsteps:
+                    issue(k + NB - 1)
+                read(k)
+                if times is not None:
+                    t1 = time.perf_counter()
+                    times.append(1000 * (t1 - ts))
+                    ts = t1
+
         # warm-up of the pipelined loop itself (3 steps), then the timed loop
         # from an empty pipeline
-        issue(0)
-        for k in range(3):
-            if k + 1 < 3:
-                issue(k + 1)
-            read(k)
+        pipelined(3)
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
         step_ms = []  # host clock from one image's read-back to the next
-        ts = t0
-        issue(0)
-        for k in range(args.e2e_steps):
-            if k + 1 < args.e2e_steps:
-                issue(k + 1)
-            read(k)
-            t1 = time.perf_counter()
-            step_ms.append(1000 * (t1 - ts))
-            ts = t1
+        pipelined(args.e2e_steps, step_ms)
         torch.cuda.synchronize()
         dt = max_over_ranks(time.perf_counter() - t0, dist)
         e2e = {"value": whole_job_rate(world, NSUB * NITER * args.e2e_steps, dt), "unit": UNIT,
@@ -529,9 +533,9 @@ def run_gpu(args) -> int:
                "step_ms": [round(x, 2) for x in step_ms],
                "median_step_ms": round(statistics.median(step_ms), 2),
                "path": "per step: gf_recon_load_async(pinned host sinogram+normalization) + gf_recon_iterate(2) + "
-                       "gf_recon_get_image(scaled); two reconstructions of one context alternate, the next "
-                       "step's upload (copy stream) and iterations queued before this step's image is read "
-                       "back",
+                       "gf_recon_get_image(scaled); three reconstructions of one context take the steps in turn, "
+                       "the next two steps' uploads (copy stream) and iterations queued before this step's "
+                       "image is read back",
                "sequential_phases": phases,
                "sequential": {"value": whole_job_rate(world, NSUB * NITER * args.e2e_steps, dt_seq),
                               "ms_per_step": 1000.0 * dt_seq / args.e2e_steps,
